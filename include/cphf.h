@@ -1,0 +1,189 @@
+/*
+ * cphf.h -- C ABI of the GB300 CPHF/CPKS response library (libcphf.so).
+ *
+ * Drop-in boundary for the CPHF response path of rstsr-showcase-hessian: the
+ * RI-J/RI-K response plugin, the numint XC response plugin, the block-Krylov
+ * solver and the CPHF driver steps around it.  Every entry point names the
+ * reference item it replaces (paths inside the reference project).
+ *
+ * Conventions
+ *  - All arrays are FP64 and col-major (F-order), as in the reference
+ *    (src/lib.rs:40-48, src/util/krylov_block.rs:13-16).  Shapes are written
+ *    [fastest, ..., slowest].
+ *  - A data pointer may point to host memory (pageable or pinned) or to device
+ *    memory of the context's GPU; the library detects which and copies
+ *    accordingly.  Inputs are borrowed for the duration of the call only.
+ *  - Orbitals are ordered occupied first (src/hessian/rscf.rs:253-254).
+ *  - Where the reference panics (check_shape!, src/util/panic_handling.rs:36-58;
+ *    non-convergence, src/util/krylov_block.rs:188-194) the call returns a
+ *    status code; cphf_last_error() gives the message.
+ *  - One context per host thread; calls on a context are serialized on the
+ *    context's CUDA stream (the reference's &mut self plugins,
+ *    src/hessian/trait_rhess.rs:637-664).
+ */
+#ifndef CPHF_H
+#define CPHF_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum cphf_status {
+  CPHF_OK = 0,
+  CPHF_ERR_SHAPE = 1,          /* shape mismatch (check_shape!) */
+  CPHF_ERR_NOT_CONVERGED = 2,  /* krylov_block failed to converge */
+  CPHF_ERR_NONFINITE = 3,      /* NaN/Inf found in an input or a residual */
+  CPHF_ERR_OOM = 4,            /* device allocation failed */
+  CPHF_ERR_CUDA = 5,           /* CUDA runtime error */
+  CPHF_ERR_TIMEOUT = 6,        /* a bounded device-side wait ran out */
+  CPHF_ERR_STATE = 7,          /* call order (e.g. response before prepare) */
+  CPHF_ERR_ARG = 8             /* invalid argument */
+} cphf_status;
+
+/* Arithmetic of the solve. */
+typedef enum cphf_precision {
+  CPHF_PRECISION_FP64 = 0,   /* every contraction in FP64 (the reference's arithmetic) */
+  CPHF_PRECISION_MIXED = 1   /* split-BF16 tensor-core operator inside FP64 defect correction */
+} cphf_precision;
+
+/* HessSCFConfig (src/hessian/rscf.rs:5-18) plus the GPU-side options. */
+typedef struct cphf_config {
+  double level_shift;        /* default 0.0 */
+  double cphf_tol;           /* default 1e-8 */
+  int64_t cphf_max_cycle;    /* default 42 */
+  int64_t cphf_max_space;    /* default 14 */
+  double cphf_lindep;        /* default 1e-14 */
+  int32_t precision;         /* cphf_precision, default CPHF_PRECISION_FP64 */
+  int32_t device;            /* CUDA device ordinal, default 0 */
+  double residual_tol;       /* mixed: stop when max column ||b-(I+A)x||_2 < residual_tol (default 1e-8) */
+  double inner_tol;          /* mixed: Krylov tol of each inner solve, relative to the residual (default 1e-6) */
+  int64_t max_refine;        /* mixed: maximum defect-correction steps (default 6) */
+  int32_t use_learned_guess; /* use the MLP initial guess / preconditioner if weights are set (default 0) */
+  int32_t verbose;           /* print per-cycle diagnostics like krylov_block.rs:148-151 (default 0) */
+  int64_t aux_chunk;         /* aux functions per K-term chunk (default 0 = automatic) */
+} cphf_config;
+
+/* Solver statistics (the reference reports them by println!, krylov_block.rs:148-151, 175). */
+typedef struct cphf_stats {
+  int64_t aop_calls;            /* operator applications inside the Krylov solver(s) */
+  int64_t aop_columns;          /* sum of the block widths of those applications */
+  int64_t cycles;               /* Krylov cycles (summed over restarts and refinement steps) */
+  int64_t restarts;             /* hard restarts */
+  double max_innerprod;         /* last max ||new trial||^2 (the reference's convergence signal) */
+  double residual_max;          /* max column 2-norm of b - (I+A)x, FP64, after the solve */
+  int64_t fp64_matvec_columns;  /* columns pushed through the FP64 operator */
+  int64_t lowp_matvec_columns;  /* columns pushed through the split-precision operator */
+  int64_t refine_steps;         /* defect-correction steps (mixed precision) */
+  double seconds;               /* wall time of the call */
+} cphf_stats;
+
+typedef struct cphf_ctx cphf_ctx;
+
+/* Operator callback for cphf_krylov_block: y[:, 0:nblock] = A x[:, 0:nblock],
+ * col-major [n, nblock] DEVICE arrays, work issued on `stream` (a cudaStream_t).
+ * Return 0 on success.  Mirrors `aop: impl FnMut(TsrView) -> Tsr`
+ * (src/util/krylov_block.rs:40). */
+typedef int (*cphf_aop_fn)(void* user, const double* x, int64_t n, int64_t nblock, double* y,
+                           void* stream);
+
+/* ---- context ---------------------------------------------------------------------------- */
+cphf_status cphf_config_default(cphf_config* cfg);
+cphf_status cphf_ctx_create(const cphf_config* cfg, cphf_ctx** out);
+cphf_status cphf_ctx_destroy(cphf_ctx* ctx);
+cphf_status cphf_ctx_set_config(cphf_ctx* ctx, const cphf_config* cfg);
+const char* cphf_status_string(cphf_status s);
+const char* cphf_last_error(const cphf_ctx* ctx);
+void* cphf_ctx_stream(const cphf_ctx* ctx);            /* the context's cudaStream_t */
+cphf_status cphf_ctx_synchronize(cphf_ctx* ctx);
+int64_t cphf_ctx_device_bytes(const cphf_ctx* ctx);   /* device memory held by the context */
+/* Number of kernels this context launched so far (launch counter, for benchmarks). */
+int64_t cphf_ctx_kernel_launches(const cphf_ctx* ctx);
+
+/* ---- RI-JK plugin ---------------------------------------------------------------------- */
+/* RHessRIJK::new_with_cderi (src/ri_jk/hess_r.rs:1774-1794) / UHessRIJK:
+ * cderi [nao*(nao+1)/2, naux], packed upper triangle, element (mu<=nu) at
+ * nu*(nu+1)/2+mu (src/util/density_matrices.rs:48-57, hess_r.rs:1725-1735). */
+cphf_status cphf_rijk_set_cderi(cphf_ctx* ctx, const double* cderi, int64_t nao, int64_t naux,
+                                double scale_j, double scale_k);
+
+/* ---- XC plugin (LDA / XCDenType::RHO, src/xceff/flags.rs:33-55) ----------------------- */
+/* RHessKSNIMatmul / UHessKSNIMatmul with intmd["cpks_fxc"] (src/numint_matmul/hess_rks.rs:814-824, 895):
+ *   ao      [ngrids, nao]  AO values (derivative order 0), the reference's get_cached_ao(0) tensor
+ *   weights [ngrids]
+ *   fxc     nspin=1: [ngrids] = fxc_eff[g,0,0];  nspin=2: [ngrids, 2, 2] = fxc_eff[g,0,s_in,0,s_out]
+ *   batch_offsets [nbatch+1] grid batches (e.g. per atom); NULL = one batch.
+ * Must be called after cphf_rijk_set_cderi or cphf_set_nao (nao is taken from there). */
+cphf_status cphf_xc_set_grid(cphf_ctx* ctx, const double* ao, const double* weights,
+                             const double* fxc, int64_t ngrids, int32_t nspin,
+                             const int64_t* batch_offsets, int64_t nbatch);
+/* Declare nao when no RI-JK plugin is used. */
+cphf_status cphf_set_nao(cphf_ctx* ctx, int64_t nao);
+
+/* ---- response preparation and response (RHessElecInteractAPI) --------------------------- */
+/* make_response_preparation (src/hessian/trait_rhess.rs:637, hess_r.rs:1911-1914,
+ * hess_rks.rs:886-889) plus the orbital energies the CPHF driver keeps (rscf.rs:21-25):
+ *   mo_coeff[s] [nao, nmo], mo_occ[s] [nmo], mo_energy[s] [nmo], s < nspin (1 = RHF/RKS, 2 = UHF/UKS). */
+cphf_status cphf_prepare(cphf_ctx* ctx, int32_t nspin, const double* const* mo_coeff,
+                         const double* const* mo_occ, const double* const* mo_energy, int64_t nmo);
+
+/* get_response_bra summed over the set plugins (rscf.rs:210-220 loop body):
+ *   bra[s], out[s] [nao, nocc_s, nprop].
+ *   RHF: hess_r.rs:1916-1953 (+ hess_rks.rs:891-908); UHF: hess_u.rs:270-313 (+ hess_uks.rs:740-764). */
+cphf_status cphf_response_bra(cphf_ctx* ctx, const double* const* bra, int64_t nprop,
+                              double* const* out);
+/* One plugin only: which = 0 RI-JK, 1 XC. */
+cphf_status cphf_plugin_response_bra(cphf_ctx* ctx, int32_t which, const double* const* bra,
+                                     int64_t nprop, double* const* out);
+
+/* ---- CPHF driver (src/hessian/rscf.rs, uscf.rs) ----------------------------------------- */
+/* response_mo (rscf.rs:210-220, uscf.rs:203-218): mo1[s], resp[s] [nmo, nocc_s, nprop]. */
+cphf_status cphf_response_mo(cphf_ctx* ctx, const double* const* mo1, int64_t nprop,
+                             double* const* resp);
+/* response_dimless_cphf (rscf.rs:237-263, uscf.rs:230-265). */
+cphf_status cphf_response_dimless(cphf_ctx* ctx, const double* const* mo1, int64_t nprop,
+                                  double* const* resp);
+/* solve_dimless_cphf (rscf.rs:278-300, uscf.rs:278-341): rhs[s], mo1[s] [nmo, nocc_s, nprop];
+ * x0 may be NULL.  FP64: krylov_block with the fused dimensionless operator.
+ * MIXED: the same solver on the split-precision operator inside FP64 defect correction. */
+cphf_status cphf_solve_dimless_cphf(cphf_ctx* ctx, const double* const* rhs, int64_t nprop,
+                                    const double* const* x0, double* const* mo1, cphf_stats* stats);
+/* finalize_cphf (rscf.rs:328-353, uscf.rs:365-406): f1mo[s], s1mo[s] [nmo, nocc_s, 3, natm];
+ * mo1[s] in/out; mo_e1[s] [nocc_s, nocc_s, 3, natm] out. */
+cphf_status cphf_finalize_cphf(cphf_ctx* ctx, const double* const* f1mo, const double* const* s1mo,
+                               int64_t natm, double* const* mo1, double* const* mo_e1);
+/* get_cphf_hess (rscf.rs:371-399, uscf.rs:408-446): de [3, 3, natm, natm]. */
+cphf_status cphf_get_cphf_hess(cphf_ctx* ctx, const double* const* f1mo, const double* const* s1mo,
+                               const double* const* mo1, const double* const* mo_e1, int64_t natm,
+                               double* de);
+
+/* ---- block Krylov solver ---------------------------------------------------------------- */
+/* krylov_block (src/util/krylov_block.rs:39-197) with a caller-supplied operator:
+ * b, x [n, nset]; x0 may be NULL. */
+cphf_status cphf_krylov_block(cphf_ctx* ctx, cphf_aop_fn aop, void* user, const double* b,
+                              const double* x0, int64_t n, int64_t nset, double tol,
+                              int64_t max_cycle, int64_t max_space, double lindep, double* x,
+                              cphf_stats* stats);
+
+/* A dense FP64 operator y = A x (A [n, n] col-major, copied to the device), usable as the
+ * aop of cphf_krylov_block: pass cphf_dense_op_apply and the op as `user`.  This is the
+ * operator of the reference's solver tests (tests/test_krylov_block.rs:18-23). */
+typedef struct cphf_dense_op cphf_dense_op;
+cphf_status cphf_dense_op_create(cphf_ctx* ctx, const double* A, int64_t n, cphf_dense_op** out);
+int cphf_dense_op_apply(void* user, const double* x, int64_t n, int64_t nblock, double* y,
+                        void* stream);
+cphf_status cphf_dense_op_destroy(cphf_dense_op* op);
+
+/* Copy `bytes` between any host / device pointers on the context's stream and wait. */
+cphf_status cphf_copy(cphf_ctx* ctx, void* dst, const void* src, int64_t bytes);
+
+/* ---- learned initial guess / preconditioner (no counterpart in the reference) ------------ */
+/* Per-(i,a)-pair MLP 3 -> 64 -> 64 -> 2 (GELU), FP32 weights packed as
+ * W1[64,3] b1[64] W2[64,64] b2[64] W3[2,64] b3[2] (row-major per matrix). */
+cphf_status cphf_mlp_set_weights(cphf_ctx* ctx, const float* weights, int64_t nweights);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CPHF_H */

@@ -1,0 +1,615 @@
+// C ABI of libcphf (include/cphf.h).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "ctx.cuh"
+#include "kernels.cuh"
+
+using namespace cphf;
+
+namespace {
+
+struct CounterScope {
+  int64_t* prev;
+  explicit CounterScope(cphf_ctx* c) : prev(g_launch_counter) { g_launch_counter = &c->launches; }
+  ~CounterScope() { g_launch_counter = prev; }
+};
+
+template <typename F>
+cphf_status guarded(cphf_ctx* c, F&& f) {
+  if (!c) return CPHF_ERR_ARG;
+  try {
+    CPHF_CUDA(cudaSetDevice(c->device));
+    CounterScope scope(c);
+    f();
+    c->last_error.clear();
+    return CPHF_OK;
+  } catch (const Error& e) {
+    c->last_error = e.what();
+    return e.status;
+  } catch (const std::exception& e) {
+    c->last_error = e.what();
+    return CPHF_ERR_CUDA;
+  }
+}
+
+// Copy `bytes` from a host or device pointer into device memory (cudaMemcpyDefault / UVA).
+void copy_in(cphf_ctx* c, void* dst, const void* src, size_t bytes) {
+  if (bytes == 0) return;
+  CPHF_CHECK_ARG(src != nullptr, "null input pointer");
+  CPHF_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, c->stream));
+}
+void copy_out(cphf_ctx* c, void* dst, const void* src, size_t bytes) {
+  if (bytes == 0) return;
+  CPHF_CHECK_ARG(dst != nullptr, "null output pointer");
+  CPHF_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, c->stream));
+}
+// Read a small array from host or device memory into a host vector.
+template <typename T>
+std::vector<T> read_small(cphf_ctx* c, const T* src, int64_t n) {
+  std::vector<T> v(n);
+  if (n == 0) return v;
+  CPHF_CHECK_ARG(src != nullptr, "null input pointer");
+  CPHF_CUDA(cudaMemcpyAsync(v.data(), src, n * sizeof(T), cudaMemcpyDefault, c->stream));
+  CPHF_CUDA(cudaStreamSynchronize(c->stream));
+  return v;
+}
+
+void require_prepared(cphf_ctx* c) {
+  if (!c->prepared) throw Error(CPHF_ERR_STATE, "cphf_prepare (make_response_preparation) has not been called");
+  if (!c->has_rijk && !c->has_xc) throw Error(CPHF_ERR_STATE, "no electron-interaction plugin is set");
+}
+
+int64_t bra_elems(cphf_ctx* c, int s, int64_t nprop) { return c->nao * c->spin[s].nocc * nprop; }
+int64_t mo_elems(cphf_ctx* c, int s, int64_t nprop) { return c->spin[s].nmo * c->spin[s].nocc * nprop; }
+
+// Staging of spin-resolved arrays into one device buffer; returns per-spin device pointers.
+void stage_in(cphf_ctx* c, DevBuf& buf, const double* const* src, const std::vector<int64_t>& elems,
+              double* dev[2]) {
+  int64_t tot = 0;
+  for (int64_t e : elems) tot += e;
+  buf.ensure((size_t)std::max<int64_t>(tot, 1) * 8, c->counter());
+  int64_t off = 0;
+  for (size_t s = 0; s < elems.size(); ++s) {
+    dev[s] = buf.as<double>() + off;
+    if (src) copy_in(c, dev[s], src[s], elems[s] * 8);
+    off += elems[s];
+  }
+}
+
+// The packed Krylov vector [n, nprop] from per-spin [nmo, nocc_s, nprop] arrays (uscf.rs:292-304).
+void pack_krylov(cphf_ctx* c, const double* const* src, int64_t nprop, double* dst) {
+  const int64_t n = krylov_n(c);
+  int64_t off = 0;
+  for (int s = 0; s < c->nspin; ++s) {
+    const int64_t len = c->spin[s].nmo * c->spin[s].nocc;
+    if (len > 0 && nprop > 0) {
+      CPHF_CHECK_ARG(src[s] != nullptr, "null input pointer");
+      CPHF_CUDA(cudaMemcpy2DAsync(dst + off, n * 8, src[s], len * 8, len * 8, nprop, cudaMemcpyDefault, c->stream));
+    }
+    off += len;
+  }
+}
+void unpack_krylov(cphf_ctx* c, const double* src, int64_t nprop, double* const* dst) {
+  const int64_t n = krylov_n(c);
+  int64_t off = 0;
+  for (int s = 0; s < c->nspin; ++s) {
+    const int64_t len = c->spin[s].nmo * c->spin[s].nocc;
+    if (len > 0 && nprop > 0) {
+      CPHF_CHECK_ARG(dst[s] != nullptr, "null output pointer");
+      CPHF_CUDA(cudaMemcpy2DAsync(dst[s], len * 8, src + off, n * 8, len * 8, nprop, cudaMemcpyDefault, c->stream));
+    }
+    off += len;
+  }
+}
+
+void check_finite(cphf_ctx* c, const double* dev, int64_t n, const char* what) {
+  c->k_info.ensure(sizeof(int), c->counter());
+  DevBuf tmp;
+  tmp.ensure(sizeof(int), c->counter());
+  CPHF_CUDA(cudaMemsetAsync(tmp.p, 0, sizeof(int), c->stream));
+  launch_count_nonfinite(dev, n, tmp.as<int>(), c->stream);
+  int bad = 0;
+  CPHF_CUDA(cudaMemcpyAsync(&bad, tmp.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CPHF_CUDA(cudaStreamSynchronize(c->stream));
+  if (bad) throw Error(CPHF_ERR_NONFINITE, std::string("non-finite values in ") + what);
+}
+
+}  // namespace
+
+namespace cphf {
+// mixed-precision solve (defined in mixed.cu)
+bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, double* x, cphf_stats* st);
+}
+
+extern "C" {
+
+cphf_status cphf_config_default(cphf_config* cfg) {
+  if (!cfg) return CPHF_ERR_ARG;
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->level_shift = 0.0;
+  cfg->cphf_tol = 1e-8;
+  cfg->cphf_max_cycle = 42;
+  cfg->cphf_max_space = 14;
+  cfg->cphf_lindep = 1e-14;
+  cfg->precision = CPHF_PRECISION_FP64;
+  cfg->device = 0;
+  cfg->residual_tol = 1e-8;
+  cfg->inner_tol = 1e-6;
+  cfg->max_refine = 6;
+  cfg->use_learned_guess = 0;
+  cfg->verbose = 0;
+  cfg->aux_chunk = 0;
+  return CPHF_OK;
+}
+
+const char* cphf_status_string(cphf_status s) {
+  switch (s) {
+    case CPHF_OK: return "ok";
+    case CPHF_ERR_SHAPE: return "shape mismatch";
+    case CPHF_ERR_NOT_CONVERGED: return "krylov_block failed to converge";
+    case CPHF_ERR_NONFINITE: return "non-finite value";
+    case CPHF_ERR_OOM: return "out of device memory";
+    case CPHF_ERR_CUDA: return "CUDA error";
+    case CPHF_ERR_TIMEOUT: return "device wait timed out";
+    case CPHF_ERR_STATE: return "invalid call order";
+    case CPHF_ERR_ARG: return "invalid argument";
+  }
+  return "unknown status";
+}
+
+cphf_status cphf_ctx_create(const cphf_config* cfg, cphf_ctx** out) {
+  if (!out) return CPHF_ERR_ARG;
+  *out = nullptr;
+  cphf_ctx* c = new cphf_ctx();
+  if (cfg) c->cfg = *cfg; else cphf_config_default(&c->cfg);
+  c->device = c->cfg.device;
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return CPHF_ERR_CUDA;
+  }
+  *out = c;
+  return CPHF_OK;
+}
+
+cphf_status cphf_ctx_destroy(cphf_ctx* c) {
+  if (!c) return CPHF_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  lowp_release(c);
+  cudaStream_t s = c->stream;
+  delete c;
+  if (s) cudaStreamDestroy(s);
+  return CPHF_OK;
+}
+
+cphf_status cphf_ctx_set_config(cphf_ctx* c, const cphf_config* cfg) {
+  return guarded(c, [&] {
+    CPHF_CHECK_ARG(cfg != nullptr, "null config");
+    CPHF_CHECK_ARG(cfg->device == c->device, "the device of a context cannot change");
+    const bool was_mixed = c->cfg.precision == CPHF_PRECISION_MIXED;
+    c->cfg = *cfg;
+    if (c->prepared && !was_mixed && cfg->precision == CPHF_PRECISION_MIXED) lowp_prepare(c);
+  });
+}
+
+const char* cphf_last_error(const cphf_ctx* c) { return c ? c->last_error.c_str() : "null context"; }
+void* cphf_ctx_stream(const cphf_ctx* c) { return c ? (void*)c->stream : nullptr; }
+int64_t cphf_ctx_device_bytes(const cphf_ctx* c) { return c ? c->device_bytes : 0; }
+int64_t cphf_ctx_kernel_launches(const cphf_ctx* c) { return c ? c->launches : 0; }
+
+cphf_status cphf_ctx_synchronize(cphf_ctx* c) {
+  return guarded(c, [&] { CPHF_CUDA(cudaStreamSynchronize(c->stream)); });
+}
+
+cphf_status cphf_set_nao(cphf_ctx* c, int64_t nao) {
+  return guarded(c, [&] {
+    CPHF_CHECK_ARG(nao > 0, "nao must be positive");
+    CPHF_CHECK_SHAPE(!c->has_rijk || c->nao == nao, "nao differs from the cderi's");
+    c->nao = nao;
+    c->prepared = false;
+  });
+}
+
+cphf_status cphf_rijk_set_cderi(cphf_ctx* c, const double* cderi, int64_t nao, int64_t naux,
+                                double scale_j, double scale_k) {
+  return guarded(c, [&] {
+    CPHF_CHECK_ARG(nao > 0 && naux > 0, "nao and naux must be positive");
+    CPHF_CHECK_SHAPE(!c->has_xc || c->nao == nao, "nao differs from the XC grid's");
+    const int64_t nao_tp = nao * (nao + 1) / 2;
+    c->nao = nao;
+    c->naux = naux;
+    c->scale_j = scale_j;
+    c->scale_k = scale_k;
+    c->cderi_tp.ensure((size_t)nao_tp * naux * 8, c->counter());
+    copy_in(c, c->cderi_tp.p, cderi, (size_t)nao_tp * naux * 8);
+    check_finite(c, c->cderi_tp.as<double>(), nao_tp * naux, "cderi");
+    c->Bd.ensure((size_t)nao * nao * naux * 8, c->counter());
+    launch_unpack_cderi(c->cderi_tp.as<double>(), nao, naux, c->Bd.as<double>(), c->stream);
+    c->has_rijk = true;
+    c->prepared = false;
+    lowp_release(c);
+    CPHF_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+cphf_status cphf_xc_set_grid(cphf_ctx* c, const double* ao, const double* weights, const double* fxc,
+                             int64_t ngrids, int32_t nspin, const int64_t* batch_offsets,
+                             int64_t nbatch) {
+  return guarded(c, [&] {
+    CPHF_CHECK_ARG(c->nao > 0, "set cderi or nao before the XC grid");
+    CPHF_CHECK_ARG(ngrids >= 0, "ngrids must be non-negative");
+    CPHF_CHECK_ARG(nspin == 1 || nspin == 2, "nspin must be 1 or 2");
+    const int64_t nao = c->nao;
+    std::vector<int64_t> off;
+    if (batch_offsets && nbatch > 0) {
+      off = read_small(c, batch_offsets, nbatch + 1);
+      CPHF_CHECK_SHAPE(off.front() == 0 && off.back() == ngrids, "batch offsets must span [0, ngrids]");
+      for (int64_t b = 0; b < nbatch; ++b) CPHF_CHECK_SHAPE(off[b] <= off[b + 1], "batch offsets must be non-decreasing");
+    } else {
+      off = {0, ngrids};
+    }
+    const int64_t nb = (int64_t)off.size() - 1;
+    // stage the dense AO block, find each batch's non-zero AO window, pack the windows
+    DevBuf dense;
+    dense.ensure((size_t)std::max<int64_t>(ngrids * nao, 1) * 8, nullptr);
+    copy_in(c, dense.p, ao, (size_t)ngrids * nao * 8);
+    // window detection on the host copy of per-(batch, column) non-zero flags
+    std::vector<int> flags((size_t)nb * nao, 0);
+    {
+      DevBuf fl;
+      fl.ensure((size_t)std::max<int64_t>(nb * nao, 1) * sizeof(int), nullptr);
+      CPHF_CUDA(cudaMemsetAsync(fl.p, 0, (size_t)nb * nao * sizeof(int), c->stream));
+      DevBuf doff;
+      doff.ensure(off.size() * 8, nullptr);
+      CPHF_CUDA(cudaMemcpyAsync(doff.p, off.data(), off.size() * 8, cudaMemcpyHostToDevice, c->stream));
+      launch_nonzero_flags(dense.as<double>(), ngrids, nao, doff.as<int64_t>(), nb, fl.as<int>(), c->stream);
+      CPHF_CUDA(cudaMemcpyAsync(flags.data(), fl.p, flags.size() * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+      CPHF_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    std::vector<XcBatch> batches(nb);
+    int64_t total = 0;
+    for (int64_t b = 0; b < nb; ++b) {
+      XcBatch& x = batches[b];
+      x.g0 = off[b];
+      x.npts = off[b + 1] - off[b];
+      int64_t lo = nao, hi = -1;
+      for (int64_t m = 0; m < nao; ++m)
+        if (flags[b * nao + m]) { lo = std::min(lo, m); hi = std::max(hi, m); }
+      if (hi < lo) { x.lo = 0; x.nwin = 0; }
+      else { x.lo = lo; x.nwin = hi - lo + 1; }
+      x.phi_off = total;
+      total += x.npts * x.nwin;
+    }
+    c->phi.ensure((size_t)std::max<int64_t>(total, 1) * 8, c->counter());
+    for (const XcBatch& x : batches) {
+      if (x.npts == 0 || x.nwin == 0) continue;
+      CPHF_CUDA(cudaMemcpy2DAsync(c->phi.as<double>() + x.phi_off, x.npts * 8,
+                                  dense.as<double>() + x.g0 + ngrids * x.lo, ngrids * 8, x.npts * 8,
+                                  x.nwin, cudaMemcpyDeviceToDevice, c->stream));
+    }
+    c->weights.ensure((size_t)std::max<int64_t>(ngrids, 1) * 8, c->counter());
+    copy_in(c, c->weights.p, weights, (size_t)ngrids * 8);
+    const int64_t nf = nspin == 1 ? ngrids : 4 * ngrids;
+    c->fxc.ensure((size_t)std::max<int64_t>(nf, 1) * 8, c->counter());
+    copy_in(c, c->fxc.p, fxc, (size_t)nf * 8);
+    CPHF_CUDA(cudaStreamSynchronize(c->stream));
+    c->xc_batches = batches;
+    c->ngrids = ngrids;
+    c->xc_nspin = nspin;
+    c->has_xc = true;
+    c->prepared = false;
+    lowp_release(c);
+  });
+}
+
+cphf_status cphf_prepare(cphf_ctx* c, int32_t nspin, const double* const* mo_coeff,
+                         const double* const* mo_occ, const double* const* mo_energy, int64_t nmo) {
+  return guarded(c, [&] {
+    CPHF_CHECK_ARG(nspin == 1 || nspin == 2, "nspin must be 1 or 2");
+    CPHF_CHECK_ARG(c->nao > 0, "set cderi or nao before the preparation");
+    CPHF_CHECK_ARG(mo_coeff && mo_occ && mo_energy, "null orbital arrays");
+    CPHF_CHECK_SHAPE(nmo > 0 && nmo <= c->nao, "nmo must be in [1, nao]");
+    CPHF_CHECK_SHAPE(!c->has_xc || c->xc_nspin == nspin, "XC grid spin count differs");
+    const int64_t nao = c->nao;
+    for (int s = 0; s < nspin; ++s) {
+      std::vector<double> occ = read_small(c, mo_occ[s], nmo);
+      int64_t nocc = 0;
+      for (int64_t p = 0; p < nmo; ++p) nocc += occ[p] > 0.0 ? 1 : 0;
+      for (int64_t p = 0; p < nmo; ++p)
+        CPHF_CHECK_SHAPE((occ[p] > 0.0) == (p < nocc), "orbitals must be ordered occupied first");
+      SpinState& sp = c->spin[s];
+      sp.nmo = nmo;
+      sp.nocc = nocc;
+      sp.C.ensure((size_t)nao * nmo * 8, c->counter());
+      copy_in(c, sp.C.p, mo_coeff[s], (size_t)nao * nmo * 8);
+      sp.e.ensure((size_t)nmo * 8, c->counter());
+      copy_in(c, sp.e.p, mo_energy[s], (size_t)nmo * 8);
+      check_finite(c, sp.C.as<double>(), nao * nmo, "mo_coeff");
+      check_finite(c, sp.e.as<double>(), nmo, "mo_energy");
+    }
+    c->nspin = nspin;
+    if (c->has_rijk) rijk_prepare(c);
+    if (c->has_xc) xc_prepare(c);
+    lowp_release(c);
+    if (c->cfg.precision == CPHF_PRECISION_MIXED) lowp_prepare(c);
+    CPHF_CUDA(cudaStreamSynchronize(c->stream));
+    c->prepared = true;
+  });
+}
+
+static cphf_status response_common(cphf_ctx* c, int which, const double* const* bra, int64_t nprop,
+                                   double* const* out) {
+  return guarded(c, [&] {
+    require_prepared(c);
+    CPHF_CHECK_ARG(bra && out, "null bra/out arrays");
+    CPHF_CHECK_SHAPE(nprop >= 0, "nprop must be non-negative");
+    if (which == 0) CPHF_CHECK_ARG(c->has_rijk, "RI-JK plugin not set");
+    if (which == 1) CPHF_CHECK_ARG(c->has_xc, "XC plugin not set");
+    std::vector<int64_t> el;
+    for (int s = 0; s < c->nspin; ++s) el.push_back(bra_elems(c, s, nprop));
+    double* din[2];
+    double* dout[2];
+    stage_in(c, c->s_host_io, bra, el, din);
+    stage_in(c, c->s_misc, nullptr, el, dout);
+    if (nprop > 0) {
+      bool acc = false;
+      if (c->has_rijk && (which < 0 || which == 0)) { rijk_response_fp64(c, din, nprop, dout, acc); acc = true; }
+      if (c->has_xc && (which < 0 || which == 1)) { xc_response_fp64(c, din, nprop, dout, acc); acc = true; }
+    }
+    for (int s = 0; s < c->nspin; ++s) copy_out(c, out[s], dout[s], el[s] * 8);
+    CPHF_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+cphf_status cphf_response_bra(cphf_ctx* c, const double* const* bra, int64_t nprop, double* const* out) {
+  return response_common(c, -1, bra, nprop, out);
+}
+
+cphf_status cphf_plugin_response_bra(cphf_ctx* c, int32_t which, const double* const* bra, int64_t nprop,
+                                     double* const* out) {
+  if (which != 0 && which != 1) return CPHF_ERR_ARG;
+  return response_common(c, which, bra, nprop, out);
+}
+
+static cphf_status response_mo_common(cphf_ctx* c, const double* const* mo1, int64_t nprop,
+                                      double* const* resp, bool dimless) {
+  return guarded(c, [&] {
+    require_prepared(c);
+    CPHF_CHECK_ARG(mo1 && resp, "null arrays");
+    const int64_t n = krylov_n(c);
+    c->s_host_io.ensure((size_t)std::max<int64_t>(n * nprop, 1) * 8 * 2, c->counter());
+    double* x = c->s_host_io.as<double>();
+    double* y = x + n * nprop;
+    pack_krylov(c, mo1, nprop, x);
+    if (nprop > 0) response_mo_fp64(c, x, nprop, y, dimless);
+    unpack_krylov(c, y, nprop, resp);
+    CPHF_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+cphf_status cphf_response_mo(cphf_ctx* c, const double* const* mo1, int64_t nprop, double* const* resp) {
+  return response_mo_common(c, mo1, nprop, resp, false);
+}
+
+cphf_status cphf_response_dimless(cphf_ctx* c, const double* const* mo1, int64_t nprop, double* const* resp) {
+  return response_mo_common(c, mo1, nprop, resp, true);
+}
+
+cphf_status cphf_solve_dimless_cphf(cphf_ctx* c, const double* const* rhs, int64_t nprop,
+                                    const double* const* x0, double* const* mo1, cphf_stats* stats) {
+  bool converged = true;
+  cphf_stats st{};
+  const auto t0 = std::chrono::steady_clock::now();
+  cphf_status rc = guarded(c, [&] {
+    require_prepared(c);
+    CPHF_CHECK_ARG(rhs && mo1, "null arrays");
+    CPHF_CHECK_SHAPE(nprop > 0, "nprop must be positive");
+    const int64_t n = krylov_n(c);
+    c->s_host_io.ensure((size_t)n * nprop * 8 * 3, c->counter());
+    double* b = c->s_host_io.as<double>();
+    double* xg = b + n * nprop;
+    double* x = xg + n * nprop;
+    pack_krylov(c, rhs, nprop, b);
+    check_finite(c, b, n * nprop, "rhs");
+    if (x0) pack_krylov(c, x0, nprop, xg);
+    if (c->cfg.precision == CPHF_PRECISION_MIXED) {
+      converged = solve_mixed(c, b, x0 ? xg : nullptr, nprop, x, &st);
+    } else {
+      KrylovParams p{c->cfg.cphf_tol, c->cfg.cphf_lindep, c->cfg.cphf_max_cycle, c->cfg.cphf_max_space,
+                     c->cfg.verbose != 0};
+      DeviceOp op = [&](const double* xin, int64_t nb, double* yout) {
+        response_mo_fp64(c, xin, nb, yout, true);
+        st.fp64_matvec_columns += nb;
+      };
+      converged = krylov_device(c, op, b, x0 ? xg : nullptr, n, nprop, p, x, &st);
+      st.residual_max = -1.0;  // not evaluated by the plain solver (the reference does not either)
+    }
+    unpack_krylov(c, x, nprop, mo1);
+    CPHF_CUDA(cudaStreamSynchronize(c->stream));
+  });
+  st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (stats) *stats = st;
+  if (rc == CPHF_OK && !converged) {
+    c->last_error = "krylov_block failed to converge";
+    return CPHF_ERR_NOT_CONVERGED;
+  }
+  return rc;
+}
+
+cphf_status cphf_finalize_cphf(cphf_ctx* c, const double* const* f1mo, const double* const* s1mo,
+                               int64_t natm, double* const* mo1, double* const* mo_e1) {
+  return guarded(c, [&] {
+    require_prepared(c);
+    CPHF_CHECK_ARG(f1mo && s1mo && mo1 && mo_e1, "null arrays");
+    CPHF_CHECK_SHAPE(natm > 0, "natm must be positive");
+    const int64_t nprop = 3 * natm, n = krylov_n(c);
+    // device layout: [mo1 | resp | f1 | s1] in Krylov packing, then per-spin mo_e1
+    int64_t ne1 = 0;
+    for (int s = 0; s < c->nspin; ++s) ne1 += c->spin[s].nocc * c->spin[s].nocc * nprop;
+    c->s_host_io.ensure((size_t)(4 * n * nprop + ne1) * 8, c->counter());
+    double* x = c->s_host_io.as<double>();
+    double* resp = x + n * nprop;
+    double* f1 = resp + n * nprop;
+    double* s1 = f1 + n * nprop;
+    double* e1 = s1 + n * nprop;
+    pack_krylov(c, mo1, nprop, x);
+    pack_krylov(c, f1mo, nprop, f1);
+    pack_krylov(c, s1mo, nprop, s1);
+    response_mo_fp64(c, x, nprop, resp, false);  // rscf.rs:342
+    int64_t off = 0, offe = 0;
+    for (int s = 0; s < c->nspin; ++s) {
+      const SpinState& sp = c->spin[s];
+      const int64_t len = sp.nmo * sp.nocc;
+      // per-spin contiguous views: copy out of the packed layout when nspin == 2
+      if (c->nspin == 1) {
+        launch_finalize(f1, s1, resp, sp.e.as<double>(), sp.nmo, sp.nocc, nprop, x, e1, c->stream);
+      } else {
+        DevBuf tmp;
+        tmp.ensure((size_t)std::max<int64_t>(len * nprop, 1) * 8 * 4, c->counter());
+        double* t0 = tmp.as<double>();
+        double* arr[4] = {t0, t0 + len * nprop, t0 + 2 * len * nprop, t0 + 3 * len * nprop};
+        const double* srcs[4] = {x, resp, f1, s1};
+        for (int k = 0; k < 4; ++k)
+          if (len > 0)
+            CPHF_CUDA(cudaMemcpy2DAsync(arr[k], len * 8, srcs[k] + off, n * 8, len * 8, nprop, cudaMemcpyDeviceToDevice, c->stream));
+        launch_finalize(arr[2], arr[3], arr[1], sp.e.as<double>(), sp.nmo, sp.nocc, nprop, arr[0], e1 + offe, c->stream);
+        if (len > 0)
+          CPHF_CUDA(cudaMemcpy2DAsync(x + off, n * 8, arr[0], len * 8, len * 8, nprop, cudaMemcpyDeviceToDevice, c->stream));
+        CPHF_CUDA(cudaStreamSynchronize(c->stream));
+      }
+      copy_out(c, mo_e1[s], e1 + offe, (size_t)sp.nocc * sp.nocc * nprop * 8);
+      off += len;
+      offe += sp.nocc * sp.nocc * nprop;
+    }
+    unpack_krylov(c, x, nprop, mo1);
+    CPHF_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+cphf_status cphf_get_cphf_hess(cphf_ctx* c, const double* const* f1mo, const double* const* s1mo,
+                               const double* const* mo1, const double* const* mo_e1, int64_t natm,
+                               double* de) {
+  return guarded(c, [&] {
+    CPHF_CHECK_ARG(c->nspin == 1 || c->nspin == 2, "cphf_prepare has not been called");
+    CPHF_CHECK_ARG(f1mo && s1mo && mo1 && mo_e1 && de, "null arrays");
+    CPHF_CHECK_SHAPE(natm > 0, "natm must be positive");
+    const int64_t nprop = 3 * natm;
+    DevBuf G;
+    G.ensure((size_t)nprop * nprop * 8 + (size_t)9 * natm * natm * 8, c->counter());
+    double* Gd = G.as<double>();
+    double* ded = Gd + nprop * nprop;
+    CPHF_CUDA(cudaMemsetAsync(Gd, 0, (size_t)nprop * nprop * 8, c->stream));
+    const double f0 = c->nspin == 1 ? 4.0 : 2.0, fs = f0, fe = c->nspin == 1 ? 2.0 : 1.0;
+    for (int s = 0; s < c->nspin; ++s) {
+      const SpinState& sp = c->spin[s];
+      const int64_t len = sp.nmo * sp.nocc * nprop, le = sp.nocc * sp.nocc * nprop;
+      DevBuf tmp;
+      tmp.ensure((size_t)std::max<int64_t>(3 * len + le, 1) * 8, c->counter());
+      double* f1 = tmp.as<double>();
+      double* s1 = f1 + len;
+      double* m1 = s1 + len;
+      double* e1 = m1 + len;
+      copy_in(c, f1, f1mo[s], len * 8);
+      copy_in(c, s1, s1mo[s], len * 8);
+      copy_in(c, m1, mo1[s], len * 8);
+      copy_in(c, e1, mo_e1[s], le * 8);
+      launch_hess_pairs(f1, s1, m1, e1, sp.e.as<double>(), sp.nmo, sp.nocc, nprop, f0, fs, fe, Gd, c->stream);
+      CPHF_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    launch_hess_assemble(Gd, natm, ded, c->stream);
+    copy_out(c, de, ded, (size_t)9 * natm * natm * 8);
+    CPHF_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+cphf_status cphf_krylov_block(cphf_ctx* c, cphf_aop_fn aop, void* user, const double* b, const double* x0,
+                              int64_t n, int64_t nset, double tol, int64_t max_cycle, int64_t max_space,
+                              double lindep, double* x, cphf_stats* stats) {
+  bool converged = true;
+  cphf_stats st{};
+  const auto t0 = std::chrono::steady_clock::now();
+  cphf_status rc = guarded(c, [&] {
+    CPHF_CHECK_ARG(aop != nullptr, "null operator");
+    CPHF_CHECK_SHAPE(n > 0 && nset > 0, "n and nset must be positive");
+    CPHF_CHECK_ARG(max_space > 0 && max_cycle >= 0, "max_space must be positive");
+    c->s_misc.ensure((size_t)n * nset * 8 * 3, c->counter());
+    double* db = c->s_misc.as<double>();
+    double* dx0 = db + n * nset;
+    double* dx = dx0 + n * nset;
+    copy_in(c, db, b, (size_t)n * nset * 8);
+    if (x0) copy_in(c, dx0, x0, (size_t)n * nset * 8);
+    KrylovParams p{tol, lindep, max_cycle, max_space, c->cfg.verbose != 0};
+    DeviceOp op = [&](const double* xin, int64_t nb, double* yout) {
+      const int r = aop(user, xin, n, nb, yout, (void*)c->stream);
+      if (r != 0) throw Error(CPHF_ERR_ARG, "operator callback returned " + std::to_string(r));
+    };
+    converged = krylov_device(c, op, db, x0 ? dx0 : nullptr, n, nset, p, dx, &st);
+    copy_out(c, x, dx, (size_t)n * nset * 8);
+    CPHF_CUDA(cudaStreamSynchronize(c->stream));
+  });
+  st.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (stats) *stats = st;
+  if (rc == CPHF_OK && !converged) {
+    c->last_error = "krylov_block failed to converge";
+    return CPHF_ERR_NOT_CONVERGED;
+  }
+  return rc;
+}
+
+struct cphf_dense_op {
+  cphf_ctx* ctx;
+  DevBuf A;
+  int64_t n;
+};
+
+cphf_status cphf_dense_op_create(cphf_ctx* c, const double* A, int64_t n, cphf_dense_op** out) {
+  return guarded(c, [&] {
+    CPHF_CHECK_ARG(out != nullptr && n > 0, "invalid dense operator arguments");
+    auto* op = new cphf_dense_op();
+    op->ctx = c;
+    op->n = n;
+    op->A.ensure((size_t)n * n * 8, nullptr);
+    copy_in(c, op->A.p, A, (size_t)n * n * 8);
+    CPHF_CUDA(cudaStreamSynchronize(c->stream));
+    *out = op;
+  });
+}
+
+int cphf_dense_op_apply(void* user, const double* x, int64_t n, int64_t nblock, double* y, void*) {
+  auto* op = static_cast<cphf_dense_op*>(user);
+  if (!op || n != op->n) return 1;
+  try {
+    GemmDesc d;
+    d.M = n; d.N = nblock; d.K = n;
+    d.A = op->A.p; d.a_m = 1; d.a_k = n;
+    d.B = x; d.b_k = 1; d.b_n = n;
+    d.C = y; d.c_m = 1; d.c_n = n;
+    gemm64(op->ctx, d);
+  } catch (const std::exception&) {
+    return 2;
+  }
+  return 0;
+}
+
+cphf_status cphf_dense_op_destroy(cphf_dense_op* op) {
+  delete op;
+  return CPHF_OK;
+}
+
+cphf_status cphf_copy(cphf_ctx* c, void* dst, const void* src, int64_t bytes) {
+  return guarded(c, [&] {
+    CPHF_CHECK_ARG(bytes >= 0, "negative size");
+    copy_out(c, dst, src, (size_t)bytes);
+    CPHF_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+}  // extern "C"

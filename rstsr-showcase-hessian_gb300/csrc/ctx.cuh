@@ -1,0 +1,135 @@
+// Context of libcphf: device-resident plugin state, scratch and the operator entry points.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <functional>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "gemm_simt.cuh"
+
+struct cphf_ctx;
+
+namespace cphf {
+
+// State of the split-precision operator (mixed.cu).
+struct LowpState {
+  DevBuf Bd32;                 // [nao, nao, naux] FP32 (SIMT fallback of the K term)
+  DevBuf Bhi, Blo;             // BF16 hi / lo split of the dense cderi for the tensor-core K term
+  int64_t ldk = 0;             // padded row length of the BF16 copies
+  DevBuf phi32;
+  DevBuf s_c1, s_resp, s_T, s_W, s_d, s_ket, s_rho, s_y, s_x, s_Thi, s_Tlo, s_acc;
+  bool use_tc = true;
+};
+
+// Learned initial guess / preconditioner weights (mlp.cu).
+struct MlpState {
+  std::vector<float> host;
+  DevBuf w;
+};
+
+struct SpinState {
+  int64_t nmo = 0, nocc = 0;
+  DevBuf C;       // [nao, nmo] FP64 (occupied columns first)
+  DevBuf e;       // [nmo] FP64
+  DevBuf Z;       // [nao, nocc, naux] FP64: Z_P = B_P Cocc
+  DevBuf O;       // [nocc, nocc, naux] FP64: O_P = Cocc^T B_P Cocc
+  DevBuf aobra;   // [ngrids, nocc] FP64: phi Cocc (XC)
+  // split-precision copies (mixed path)
+  DevBuf C32, Z32, O32, aobra32;
+};
+
+struct XcBatch {
+  int64_t g0 = 0, npts = 0;   // grid rows [g0, g0 + npts)
+  int64_t lo = 0, nwin = 0;   // AO window [lo, lo + nwin)
+  int64_t phi_off = 0;        // element offset of the batch block in phi
+};
+
+// Operator over Krylov columns: y[:, 0:nb] = A x[:, 0:nb] with device pointers, ld = n.
+using DeviceOp = std::function<void(const double* x, int64_t nb, double* y)>;
+
+}  // namespace cphf
+
+struct cphf_ctx {
+  cphf_config cfg{};
+  int device = 0;
+  int num_sms = 152;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  int64_t device_bytes = 0;
+  int64_t launches = 0;
+
+  // RI-JK plugin
+  bool has_rijk = false;
+  int64_t nao = 0, naux = 0;
+  double scale_j = 0.0, scale_k = 0.0;
+  cphf::DevBuf cderi_tp;  // [nao_tp, naux]
+  cphf::DevBuf Bd;        // [nao, nao, naux] dense FP64
+
+  // XC plugin
+  bool has_xc = false;
+  int xc_nspin = 1;
+  int64_t ngrids = 0;
+  std::vector<cphf::XcBatch> xc_batches;
+  cphf::DevBuf phi, weights, fxc;  // phi: batch blocks [npts_b, nwin_b] (grid fastest)
+  cphf::DevBuf phi32;
+
+  // prepared orbitals
+  bool prepared = false;
+  int nspin = 0;
+  cphf::SpinState spin[2];
+
+  // scratch (grown on demand)
+  cphf::DevBuf ws_gemm, s_c1, s_resp, s_T, s_W, s_d, s_ket, s_rho, s_y, s_x, s_misc, s_host_io;
+  cphf::DevBuf k_xs, k_ax, k_h, k_g, k_b, k_xacc, k_x1, k_axt, k_coef, k_ip, k_keep, k_part, k_idx,
+      k_hw, k_info, k_r, k_norm;
+
+  std::unique_ptr<cphf::LowpState> lowp;
+  std::unique_ptr<cphf::MlpState> mlp;
+
+  int64_t* counter() { return &device_bytes; }
+};
+
+namespace cphf {
+
+// gemm helpers bound to the context (stream, split-K workspace, SM count)
+void gemm64(cphf_ctx* c, const GemmDesc& d);
+void gemm32(cphf_ctx* c, const GemmDesc& d);  // float compute, float operands/output
+template <typename TA, typename TB, typename TC>
+void gemm32x(cphf_ctx* c, const GemmDesc& d);
+
+// plugins (device pointers): bra[s], out[s] [nao, nocc_s, nb] contiguous
+void rijk_response_fp64(cphf_ctx* c, const double* const* bra, int64_t nb, double* const* out,
+                        bool accumulate);
+void xc_response_fp64(cphf_ctx* c, const double* const* bra, int64_t nb, double* const* out,
+                      bool accumulate);
+void rijk_prepare(cphf_ctx* c);
+void xc_prepare(cphf_ctx* c);
+
+// response_mo / dimensionless operator over the packed Krylov layout
+// x, y: [n, nb] with n = sum_s nmo*nocc_s.
+void response_mo_fp64(cphf_ctx* c, const double* x, int64_t nb, double* resp_mo, bool dimless);
+void response_mo_lowp(cphf_ctx* c, const double* x, int64_t nb, double* resp_mo);
+int64_t krylov_n(const cphf_ctx* c);
+
+// krylov_block on the device (src/util/krylov_block.rs:39-197)
+struct KrylovParams {
+  double tol, lindep;
+  int64_t max_cycle, max_space;
+  bool verbose;
+};
+// returns true if converged; b, x0 (nullable), x: device [n, nset]
+bool krylov_device(cphf_ctx* c, const DeviceOp& aop, const double* b, const double* x0, int64_t n,
+                   int64_t nset, const KrylovParams& p, double* x, cphf_stats* st);
+
+// max column 2-norm of b - (I + A) x with the FP64 operator; r receives the residual
+double fp64_residual(cphf_ctx* c, const double* b, const double* x, int64_t nset, double* r,
+                     cphf_stats* st);
+
+// mixed-precision support
+void lowp_prepare(cphf_ctx* c);
+void lowp_release(cphf_ctx* c);
+
+}  // namespace cphf

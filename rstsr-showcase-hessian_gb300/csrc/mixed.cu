@@ -1,0 +1,327 @@
+// Split-precision CPHF operator and the FP64 defect-correction solve.
+//
+// The operator is the same sequence of contractions as the FP64 path (rijk.cu, xc.cu,
+// operator.cu) with FP32 operands and accumulation; the dominant K-term contraction
+// B_P bra O_P runs on the tensor cores as a three-product split-BF16 GEMM with FP32
+// accumulation in TMEM (tc_gemm.cu).  Its error (~1e-6 relative) is removed by defect
+// correction: each step solves (I + A_lowp) d = r with the device Krylov solver (FP64
+// basis, orthogonalisation and projected solve), then recomputes r = b - (I + A) x with
+// the FP64 operator, until max_j ||r_j||_2 < residual_tol.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "ctx.cuh"
+#include "kernels.cuh"
+#include "tc_gemm.cuh"
+
+namespace cphf {
+
+
+void lowp_release(cphf_ctx* c) { c->lowp.reset(); }
+
+void lowp_prepare(cphf_ctx* c) {
+  if (!c->lowp) c->lowp.reset(new LowpState());
+  LowpState& L = *c->lowp;
+  const int64_t nao = c->nao, naux = c->naux;
+  if (c->has_rijk) {
+    L.use_tc = tc_available(c);
+    if (L.use_tc) {
+      tc_prepare_cderi(c, L.Bhi, L.Blo, L.ldk);
+    } else {
+      L.Bd32.ensure((size_t)nao * nao * naux * 4, c->counter());
+      launch_to_f32(c->Bd.as<double>(), nao * nao * naux, L.Bd32.as<float>(), c->stream);
+    }
+  }
+  for (int s = 0; s < c->nspin; ++s) {
+    SpinState& sp = c->spin[s];
+    sp.C32.ensure((size_t)nao * sp.nmo * 4, c->counter());
+    launch_to_f32(sp.C.as<double>(), nao * sp.nmo, sp.C32.as<float>(), c->stream);
+    if (c->has_rijk) {
+      sp.Z32.ensure((size_t)nao * sp.nocc * naux * 4, c->counter());
+      launch_to_f32(sp.Z.as<double>(), nao * sp.nocc * naux, sp.Z32.as<float>(), c->stream);
+      sp.O32.ensure((size_t)sp.nocc * sp.nocc * naux * 4, c->counter());
+      launch_to_f32(sp.O.as<double>(), sp.nocc * sp.nocc * naux, sp.O32.as<float>(), c->stream);
+    }
+    if (c->has_xc) {
+      sp.aobra32.ensure((size_t)c->ngrids * std::max<int64_t>(sp.nocc, 1) * 4, c->counter());
+      launch_to_f32(sp.aobra.as<double>(), c->ngrids * sp.nocc, sp.aobra32.as<float>(), c->stream);
+    }
+  }
+  if (c->has_xc) {
+    const int64_t tot = c->phi.bytes / 8;
+    L.phi32.ensure((size_t)std::max<int64_t>(tot, 1) * 4, c->counter());
+    launch_to_f32(c->phi.as<double>(), tot, L.phi32.as<float>(), c->stream);
+  }
+}
+
+static int64_t k_chunk_lowp(const cphf_ctx* c, int64_t no, int64_t nb) {
+  if (c->cfg.aux_chunk > 0) return std::min<int64_t>(c->cfg.aux_chunk, c->naux);
+  const int64_t per = c->nao * no * nb * 4;
+  int64_t np = std::max<int64_t>(1, (int64_t(1) << 30) / std::max<int64_t>(per, 1));
+  np = std::min<int64_t>(np, std::max<int64_t>(1, 65535 / std::max<int64_t>(nb, 1)));
+  return std::min<int64_t>(np, c->naux);
+}
+
+static void rijk_response_lowp(cphf_ctx* c, float* const* bra, int64_t nb, float* const* out) {
+  LowpState& L = *c->lowp;
+  const int64_t nao = c->nao, naux = c->naux;
+  const int ns = c->nspin;
+  bool written[2] = {false, false};
+  if (c->scale_j != 0.0) {
+    L.s_d.ensure((size_t)naux * nb * 4, c->counter());
+    for (int s = 0; s < ns; ++s) {
+      const int64_t no = c->spin[s].nocc;
+      if (no == 0) {
+        if (s == 0) CPHF_CUDA(cudaMemsetAsync(L.s_d.p, 0, (size_t)naux * nb * 4, c->stream));
+        continue;
+      }
+      GemmDesc d;
+      d.M = naux; d.N = nb; d.K = nao * no;
+      d.A = c->spin[s].Z32.p; d.a_m = nao * no; d.a_k = 1;
+      d.B = bra[s]; d.b_k = 1; d.b_n = nao * no;
+      d.C = L.s_d.p; d.c_m = 1; d.c_n = naux;
+      d.alpha = 2.0; d.beta = s == 0 ? 0.0 : 1.0;
+      gemm32(c, d);
+    }
+    const double jfac = ns == 1 ? c->scale_j : 0.5 * c->scale_j;
+    for (int s = 0; s < ns; ++s) {
+      const int64_t no = c->spin[s].nocc;
+      if (no == 0) continue;
+      GemmDesc j;
+      j.M = nao * no; j.N = nb; j.K = naux;
+      j.A = c->spin[s].Z32.p; j.a_m = 1; j.a_k = nao * no;
+      j.B = L.s_d.p; j.b_k = 1; j.b_n = naux;
+      j.C = out[s]; j.c_m = 1; j.c_n = nao * no;
+      j.alpha = 2.0 * jfac; j.beta = 0.0;
+      gemm32(c, j);
+      written[s] = true;
+    }
+  }
+  if (c->scale_k != 0.0) {
+    for (int s = 0; s < ns; ++s) {
+      const SpinState& sp = c->spin[s];
+      const int64_t no = sp.nocc;
+      if (no == 0) continue;
+      if (!written[s]) {
+        CPHF_CUDA(cudaMemsetAsync(out[s], 0, (size_t)nao * no * nb * 4, c->stream));
+        written[s] = true;
+      }
+      const int64_t np_max = k_chunk_lowp(c, no, nb);
+      if (L.use_tc) {
+        // term 1 on the tensor cores: out += -scale_k sum_P B_P (bra O_P)
+        tc_k_term1(c, L.Bhi, L.Blo, L.ldk, sp.O32.as<float>(), bra[s], no, nb, -c->scale_k, out[s],
+                   L.s_Thi, L.s_Tlo);
+      }
+      L.s_T.ensure((size_t)nao * np_max * no * nb * 4, c->counter());
+      L.s_W.ensure((size_t)no * np_max * no * nb * 4, c->counter());
+      for (int64_t P0 = 0; P0 < naux; P0 += np_max) {
+        const int64_t np = std::min<int64_t>(np_max, naux - P0);
+        if (!L.use_tc) {
+          GemmDesc t;
+          t.M = nao; t.N = no; t.K = no; t.batch1 = np; t.batch2 = nb;
+          t.A = bra[s]; t.a_m = 1; t.a_k = nao; t.a_b1 = 0; t.a_b2 = nao * no;
+          t.B = sp.O32.as<float>() + P0 * no * no; t.b_k = 1; t.b_n = no; t.b_b1 = no * no; t.b_b2 = 0;
+          t.C = L.s_T.p; t.c_m = 1; t.c_n = nao * np; t.c_b1 = nao; t.c_b2 = nao * np * no;
+          gemm32(c, t);
+          GemmDesc k1;
+          k1.M = nao; k1.N = no * nb; k1.K = nao * np;
+          k1.A = L.Bd32.as<float>() + P0 * nao * nao; k1.a_m = 1; k1.a_k = nao;
+          k1.B = L.s_T.p; k1.b_k = 1; k1.b_n = nao * np;
+          k1.C = out[s]; k1.c_m = 1; k1.c_n = nao;
+          k1.alpha = -c->scale_k; k1.beta = 1.0;
+          gemm32(c, k1);
+        }
+        GemmDesc w;
+        w.M = no; w.N = no; w.K = nao; w.batch1 = np; w.batch2 = nb;
+        w.A = sp.Z32.as<float>() + P0 * nao * no; w.a_m = nao; w.a_k = 1; w.a_b1 = nao * no; w.a_b2 = 0;
+        w.B = bra[s]; w.b_k = 1; w.b_n = nao; w.b_b1 = 0; w.b_b2 = nao * no;
+        w.C = L.s_W.p; w.c_m = no * np; w.c_n = 1; w.c_b1 = no; w.c_b2 = no * np * no;
+        gemm32(c, w);
+        GemmDesc k2;
+        k2.M = nao; k2.N = no * nb; k2.K = no * np;
+        k2.A = sp.Z32.as<float>() + P0 * nao * no; k2.a_m = 1; k2.a_k = nao;
+        k2.B = L.s_W.p; k2.b_k = 1; k2.b_n = no * np;
+        k2.C = out[s]; k2.c_m = 1; k2.c_n = nao;
+        k2.alpha = -c->scale_k; k2.beta = 1.0;
+        gemm32(c, k2);
+      }
+    }
+  }
+  for (int s = 0; s < ns; ++s)
+    if (!written[s] && c->spin[s].nocc > 0)
+      CPHF_CUDA(cudaMemsetAsync(out[s], 0, (size_t)nao * c->spin[s].nocc * nb * 4, c->stream));
+}
+
+static void xc_response_lowp(cphf_ctx* c, float* const* bra, int64_t nb, float* const* out, bool accumulate) {
+  LowpState& L = *c->lowp;
+  const int ns = c->nspin;
+  const int64_t nao = c->nao;
+  if (!accumulate)
+    for (int s = 0; s < ns; ++s)
+      if (c->spin[s].nocc > 0) CPHF_CUDA(cudaMemsetAsync(out[s], 0, (size_t)nao * c->spin[s].nocc * nb * 4, c->stream));
+  int64_t max_pts = 0;
+  for (const XcBatch& b : c->xc_batches) max_pts = std::max(max_pts, b.npts);
+  int64_t ket_per_spin = 0;
+  for (int s = 0; s < ns; ++s) ket_per_spin = std::max(ket_per_spin, max_pts * c->spin[s].nocc * nb);
+  L.s_ket.ensure((size_t)std::max<int64_t>(1, ket_per_spin * ns) * 4, c->counter());
+  L.s_rho.ensure((size_t)std::max<int64_t>(1, max_pts * nb * 2) * 4, c->counter());
+  const double fac = ns == 1 ? 4.0 : 2.0;
+  float* ket = L.s_ket.as<float>();
+  float* rho = L.s_rho.as<float>();
+  for (const XcBatch& b : c->xc_batches) {
+    if (b.npts == 0 || b.nwin == 0) continue;
+    const float* phi = L.phi32.as<float>() + b.phi_off;
+    for (int s = 0; s < ns; ++s) {
+      const int64_t no = c->spin[s].nocc;
+      float* ket_s = ket + s * ket_per_spin;
+      float* rho_s = rho + s * b.npts * nb;
+      if (no == 0) {
+        CPHF_CUDA(cudaMemsetAsync(rho_s, 0, (size_t)b.npts * nb * 4, c->stream));
+        continue;
+      }
+      GemmDesc d;
+      d.M = b.npts; d.N = no * nb; d.K = b.nwin;
+      d.A = phi; d.a_m = 1; d.a_k = b.npts;
+      d.B = bra[s] + b.lo; d.b_k = 1; d.b_n = nao;
+      d.C = ket_s; d.c_m = 1; d.c_n = b.npts;
+      gemm32(c, d);
+      launch_xc_rho<float>(c->spin[s].aobra32.as<float>() + b.g0, c->ngrids, ket_s, b.npts, no, nb, rho_s,
+                           b.npts, c->stream);
+    }
+    for (int s = 0; s < ns; ++s) {
+      const int64_t no = c->spin[s].nocc;
+      if (no == 0) continue;
+      float* ket_s = ket + s * ket_per_spin;
+      launch_xc_q<float>(c->spin[s].aobra32.as<float>() + b.g0, c->ngrids, c->weights.as<double>() + b.g0,
+                         c->fxc.as<double>() + b.g0, c->ngrids, ns, s, rho, b.npts, b.npts * nb, b.npts, no,
+                         nb, ket_s, c->stream);
+      GemmDesc d;
+      d.M = b.nwin; d.N = no * nb; d.K = b.npts;
+      d.A = phi; d.a_m = b.npts; d.a_k = 1;
+      d.B = ket_s; d.b_k = 1; d.b_n = b.npts;
+      d.C = out[s] + b.lo; d.c_m = 1; d.c_n = nao;
+      d.alpha = fac; d.beta = 1.0;
+      gemm32(c, d);
+    }
+  }
+}
+
+void response_mo_lowp(cphf_ctx* c, const double* x, int64_t nb, double* y) {
+  LowpState& L = *c->lowp;
+  const int ns = c->nspin;
+  const int64_t nao = c->nao, n = krylov_n(c);
+  int64_t tot_occ = 0, max_occ = 0, max_nmo = 0;
+  for (int s = 0; s < ns; ++s) {
+    tot_occ += c->spin[s].nocc;
+    max_occ = std::max(max_occ, c->spin[s].nocc);
+    max_nmo = std::max(max_nmo, c->spin[s].nmo);
+  }
+  L.s_c1.ensure((size_t)nao * tot_occ * nb * 4, c->counter());
+  L.s_resp.ensure((size_t)nao * tot_occ * nb * 4, c->counter());
+  L.s_y.ensure((size_t)max_nmo * max_occ * nb * 4, c->counter());
+  if (ns == 2) L.s_x.ensure((size_t)n * nb * 8, c->counter());
+  float* c1[2] = {nullptr, nullptr};
+  float* rb[2] = {nullptr, nullptr};
+  const double* xs[2] = {nullptr, nullptr};
+  int64_t off_occ = 0, off_x = 0;
+  for (int s = 0; s < ns; ++s) {
+    const SpinState& sp = c->spin[s];
+    c1[s] = L.s_c1.as<float>() + nao * off_occ * nb;
+    rb[s] = L.s_resp.as<float>() + nao * off_occ * nb;
+    off_occ += sp.nocc;
+    const int64_t len = sp.nmo * sp.nocc;
+    if (ns == 1) {
+      xs[s] = x;
+    } else {
+      double* dst = L.s_x.as<double>() + off_x * nb;
+      if (len > 0)
+        CPHF_CUDA(cudaMemcpy2DAsync(dst, len * 8, x + off_x, n * 8, len * 8, nb, cudaMemcpyDeviceToDevice, c->stream));
+      xs[s] = dst;
+    }
+    off_x += len;
+    if (sp.nocc == 0) continue;
+    GemmDesc d;
+    d.M = nao; d.N = sp.nocc * nb; d.K = sp.nmo;
+    d.A = sp.C32.p; d.a_m = 1; d.a_k = nao;
+    d.B = xs[s]; d.b_k = 1; d.b_n = sp.nmo;
+    d.C = c1[s]; d.c_m = 1; d.c_n = nao;
+    gemm32x<float, double, float>(c, d);
+  }
+  bool acc = false;
+  if (c->has_rijk) { rijk_response_lowp(c, c1, nb, rb); acc = true; }
+  if (c->has_xc) { xc_response_lowp(c, c1, nb, rb, acc); acc = true; }
+  off_x = 0;
+  for (int s = 0; s < ns; ++s) {
+    const SpinState& sp = c->spin[s];
+    const int64_t no = sp.nocc, nmo = sp.nmo, nvir = nmo - no;
+    double* yo = y + off_x;
+    off_x += nmo * no;
+    if (no == 0) continue;
+    if (nvir > 0) {
+      GemmDesc d;
+      d.M = nvir; d.N = no * nb; d.K = nao;
+      d.A = sp.C32.as<float>() + no * nao; d.a_m = nao; d.a_k = 1;
+      d.B = rb[s]; d.b_k = 1; d.b_n = nao;
+      d.C = L.s_y.p; d.c_m = 1; d.c_n = nvir;
+      gemm32(c, d);
+    }
+    launch_dimless_f32(L.s_y.as<float>(), xs[s], ns == 1 ? n : nmo * no, sp.e.as<double>(), nmo, no, nb,
+                       c->cfg.level_shift, yo, n, c->stream);
+  }
+}
+
+bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, double* x, cphf_stats* st) {
+  if (!c->lowp) lowp_prepare(c);
+  const int64_t n = krylov_n(c);
+  // refinement vectors r, rr (scaled residual), d (correction), FP64
+  DevBuf& buf = c->k_r;
+  buf.ensure((size_t)n * nset * 8 * 3, c->counter());
+  double* r = buf.as<double>();
+  double* rr = r + n * nset;
+  double* dlt = rr + n * nset;
+  cudaStream_t s = c->stream;
+  CPHF_CUDA(cudaMemsetAsync(x, 0, n * nset * 8, s));
+  CPHF_CUDA(cudaMemcpyAsync(r, b, n * nset * 8, cudaMemcpyDeviceToDevice, s));
+  // column norms of b
+  c->k_norm.ensure((size_t)(nset + residual_partials_size(n, nset)) * 8, c->counter());
+  std::vector<double> h(nset);
+  {
+    CPHF_CUDA(cudaMemsetAsync(dlt, 0, n * nset * 8, s));
+    launch_residual_norms(b, dlt, dlt, rr, n, nset, c->k_norm.as<double>(), c->k_norm.as<double>() + nset, s);
+    CPHF_CUDA(cudaMemcpyAsync(h.data(), c->k_norm.p, nset * 8, cudaMemcpyDeviceToHost, s));
+    CPHF_CUDA(cudaStreamSynchronize(s));
+  }
+  double res = 0.0;
+  for (double v : h) res = std::max(res, std::sqrt(v));
+  const KrylovParams p{c->cfg.inner_tol, c->cfg.cphf_lindep, c->cfg.cphf_max_cycle, c->cfg.cphf_max_space,
+                       c->cfg.verbose != 0};
+  DeviceOp op = [&](const double* xin, int64_t nb, double* yout) {
+    response_mo_lowp(c, xin, nb, yout);
+    st->lowp_matvec_columns += nb;
+  };
+  bool done = res < c->cfg.residual_tol;
+  for (int64_t step = 0; step < c->cfg.max_refine && !done; ++step) {
+    // solve (I + A_lowp) d' = r / |r|  (relative tolerances), x += |r| d'
+    const double scale = res > 0.0 ? res : 1.0;
+    launch_axpby(1.0 / scale, r, 0.0, rr, n * nset, s);
+    const double* g0 = nullptr;
+    if (step == 0 && x0) {
+      launch_axpby(1.0 / scale, x0, 0.0, x, n * nset, s);  // initial guess in scaled units
+      CPHF_CUDA(cudaMemcpyAsync(r, x, n * nset * 8, cudaMemcpyDeviceToDevice, s));
+      g0 = r;
+    }
+    krylov_device(c, op, rr, g0, n, nset, p, dlt, st);
+    if (step == 0 && x0) CPHF_CUDA(cudaMemsetAsync(x, 0, n * nset * 8, s));
+    launch_axpby(scale, dlt, 1.0, x, n * nset, s);
+    res = fp64_residual(c, b, x, nset, r, st);
+    st->refine_steps += 1;
+    if (c->cfg.verbose) std::printf("defect correction step %lld: max ||b - (I+A)x|| = %.3e\n", (long long)step + 1, res);
+    done = res < c->cfg.residual_tol;
+  }
+  st->residual_max = res;
+  return done;
+}
+
+}  // namespace cphf

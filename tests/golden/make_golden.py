@@ -1,0 +1,216 @@
+"""Generate the golden vectors under tests/golden/ from the reference's own Python code.
+
+Run in a container where the reference project is mounted (default path below, or the
+``CPHF_REFERENCE`` environment variable).  Nothing at test time reads the reference: the
+tests only load the ``.npz`` files written here.
+
+What runs, all from the reference's sources:
+
+* ``prototype/02-7-krylov_testing_setup.py`` -- ``build_test_system(n=40, nrhs=12)``, the
+  fixture generator of ``tests/test_krylov_block.rs`` -- and ``pyhessref/krylov_block.py``
+  on it with the Rust tests' parameters (``tol=1e-10``; ``max_space`` 6 and 3).
+* ``pyhessref/rijk/hess_restricted_naive.get_rijk_response_bra_naive`` and
+  ``pyhessref/rijk/hess_unrestricted_naive.get_uijk_response_bra_naive`` on seeded
+  synthetic systems: PySCF is absent, so a stub ``pyscf`` package is installed whose
+  integral hooks return the synthetic factor -- ``int3c2e`` -> dense ``B[mu, nu, P]`` and
+  ``int2c2e`` -> identity -- making ``(uv|P)(P|Q)^-1(Q|kl) = sum_P B_P,uv B_P,kl``.
+* ``pyhessref/hess_scf_restricted.RHessSCF`` and ``hess_scf_unrestricted.UHessSCF``
+  (``response_dimless_cphf``, ``solve_dimless_cphf``, ``finalize_cphf``,
+  ``get_cphf_hess``) driven by those naive plugins.
+
+Usage: ``python tests/golden/make_golden.py``
+"""
+
+import importlib.util
+import os
+import sys
+import types
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+REF = Path(os.environ.get("CPHF_REFERENCE", "/root/reference"))
+sys.path.insert(0, str(REPO / "rstsr-showcase-hessian_gb300"))
+
+from cphf_gb300 import synth  # noqa: E402
+
+
+class _FakeMol:
+    def __init__(self, nao, natm):
+        self.nao = nao
+        self.natm = natm
+
+    def nao_nr(self):
+        return self.nao
+
+
+_CURRENT = {}
+
+
+def _install_stub_pyscf():
+    """A minimal ``pyscf`` so that pyhessref imports; integrals come from ``_CURRENT``."""
+    pyscf = types.ModuleType("pyscf")
+    gto = types.ModuleType("pyscf.gto")
+    gto.Mole = _FakeMol
+    df = types.ModuleType("pyscf.df")
+    grad = types.ModuleType("pyscf.df.grad")
+    rhf = types.ModuleType("pyscf.df.grad.rhf")
+
+    def _int3c_wrapper(mol, aux, intor, aosym):
+        assert intor == "int3c2e" and aosym == "s1"
+        return lambda: _CURRENT["int3c2e"]
+
+    rhf._int3c_wrapper = _int3c_wrapper
+    pyscf.gto, pyscf.df, df.grad, grad.rhf = gto, df, grad, rhf
+    for name, mod in {"pyscf": pyscf, "pyscf.gto": gto, "pyscf.df": df, "pyscf.df.grad": grad,
+                      "pyscf.df.grad.rhf": rhf}.items():
+        sys.modules[name] = mod
+
+
+class _FakeAux:
+    def __init__(self, naux):
+        self.naux = naux
+
+    def intor(self, name):
+        assert name == "int2c2e"
+        return np.eye(self.naux)
+
+
+def _load_file(path, name):
+    spec = importlib.util.spec_from_file_location(name, path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _dense_b(s):
+    nao = s.nao
+    mu = np.concatenate([np.arange(nu + 1) for nu in range(nao)])
+    nu = np.concatenate([np.full(nu + 1, nu) for nu in range(nao)])
+    cd = np.zeros((nao, nao, s.naux))
+    cd[mu, nu] = s.cderi
+    cd[nu, mu] = s.cderi
+    return cd
+
+
+def _to_py(a):
+    """[nmo, nocc, 3, natm] (col-major meaning) -> pyhessref's [natm, 3, nmo, nocc]."""
+    return np.ascontiguousarray(np.transpose(a, (3, 2, 0, 1)))
+
+
+def _from_py(a):
+    return np.asfortranarray(np.transpose(a, (2, 3, 1, 0)))
+
+
+def krylov_golden():
+    # The setup script imports `krylov_block` from its own directory; load it with that on the path.
+    sys.path.insert(0, str(REF / "prototype"))
+    try:
+        setup = _load_file(REF / "prototype" / "02-7-krylov_testing_setup.py", "krylov_testing_setup")
+    finally:
+        sys.path.pop(0)
+    kb = _load_file(REF / "pyhessref" / "krylov_block.py", "pyhessref_krylov_block")
+    A, b, eigs = setup.build_test_system(n=40, nrhs=12)
+    x_ref = np.linalg.solve(np.eye(40) + A, b.T).T
+    out = dict(A=A, b=b, x_ref=x_ref, eigs=eigs)
+    for ms, mc in [(6, 30), (3, 60)]:
+        calls = [0]
+
+        def aop(x):
+            calls[0] += 1
+            return (A @ x.T).T
+
+        x = kb.krylov_block(aop, b, tol=1e-10, max_cycle=mc, max_space=ms, lindep=1e-13)
+        out[f"x_ms{ms}"] = x
+        out[f"calls_ms{ms}"] = np.array(calls[0])
+    np.savez(HERE / "krylov_fixture.npz", **out)
+
+
+def rhf_golden(name, seed):
+    from pyhessref.hess_scf_restricted import RHessSCF
+    from pyhessref.rijk.hess_restricted_naive import get_rijk_response_bra_naive
+
+    s = synth.make_system(name, seed=seed)
+    C, occ, e = s.mo_coeff[0], s.mo_occ[0], s.mo_energy[0]
+    mol, aux = _FakeMol(s.nao, s.natm), _FakeAux(s.naux)
+    _CURRENT["int3c2e"] = _dense_b(s)
+
+    class Plugin:
+        def make_response_preparation(self, mo_coeff, mo_occ):
+            self.mo_coeff, self.mo_occ = mo_coeff, mo_occ
+
+        def get_response_bra(self, bra):
+            return get_rijk_response_bra_naive(mol, aux, self.mo_coeff, self.mo_occ, bra,
+                                               scale_j=s.scale_j, scale_k=s.scale_k)
+
+    plug = Plugin()
+    drv = RHessSCF(mol, C, occ, e, None, [], [plug])
+    drv.make_response_preparation(C, occ)
+    rng = np.random.default_rng(seed + 100)
+    bra_probe = rng.standard_normal((s.nao, s.nocc[0], 5))
+    resp_probe = plug.get_response_bra(np.ascontiguousarray(np.transpose(bra_probe, (2, 0, 1))))
+    rhs_py = _to_py(s.rhs[0])
+    mo1_py = drv.solve_dimless_cphf(rhs_py.copy())
+    pre = {"f1mo": _to_py(s.f1mo[0]), "s1mo": _to_py(s.s1mo[0]), "rhs": rhs_py}
+    fin = drv.finalize_cphf(mo1_py.copy(), pre)
+    de_py = drv.get_cphf_hess(pre["f1mo"], pre["s1mo"], fin["mo1"], fin["mo_e1"])
+    np.savez(HERE / f"{name}_seed{seed}.npz",
+             cderi=s.cderi, mo_coeff=C, mo_occ=occ, mo_energy=e, rhs=s.rhs[0], f1mo=s.f1mo[0],
+             s1mo=s.s1mo[0], scale_j=s.scale_j, scale_k=s.scale_k, natm=s.natm,
+             bra_probe=bra_probe, resp_probe=np.asfortranarray(np.transpose(resp_probe, (1, 2, 0))),
+             mo1_solved=_from_py(mo1_py), mo1=_from_py(fin["mo1"]),
+             mo_e1=_from_py(fin["mo_e1"]), de_cphf=np.asfortranarray(np.transpose(de_py, (3, 2, 1, 0))))
+
+
+def uhf_golden(dims, tag, seed):
+    from pyhessref.hess_scf_unrestricted import UHessSCF
+    from pyhessref.rijk.hess_unrestricted_naive import get_uijk_response_bra_naive
+
+    s = synth.make_system(dims, seed=seed)
+    mol, aux = _FakeMol(s.nao, s.natm), _FakeAux(s.naux)
+    _CURRENT["int3c2e"] = _dense_b(s)
+    C = np.stack(s.mo_coeff)
+    occ = np.stack(s.mo_occ)
+    e = np.stack(s.mo_energy)
+
+    class Plugin:
+        def make_response_preparation(self, mo_coeff, mo_occ):
+            self.mo_coeff, self.mo_occ = mo_coeff, mo_occ
+
+        def get_response_bra(self, bra):
+            return get_uijk_response_bra_naive(mol, aux, self.mo_coeff, self.mo_occ, bra,
+                                               scale_j=s.scale_j, scale_k=s.scale_k)
+
+    plug = Plugin()
+    drv = UHessSCF(mol, C, occ, e, None, [], [plug])
+    drv.make_response_preparation(C, occ)
+    rhs_py = [_to_py(r) for r in s.rhs]
+    mo1_py = drv.solve_dimless_cphf([r.copy() for r in rhs_py])
+    pre = {"f1mo": [_to_py(f) for f in s.f1mo], "s1mo": [_to_py(x) for x in s.s1mo], "rhs": rhs_py}
+    fin = drv.finalize_cphf([m.copy() for m in mo1_py], pre)
+    de_py = drv.get_cphf_hess(pre["f1mo"], pre["s1mo"], fin["mo1"], fin["mo_e1"])
+    out = dict(cderi=s.cderi, scale_j=s.scale_j, scale_k=s.scale_k, natm=s.natm,
+               de_cphf=np.asfortranarray(np.transpose(de_py, (3, 2, 1, 0))))
+    for sp in range(2):
+        out.update({f"mo_coeff{sp}": s.mo_coeff[sp], f"mo_occ{sp}": s.mo_occ[sp],
+                    f"mo_energy{sp}": s.mo_energy[sp], f"rhs{sp}": s.rhs[sp], f"f1mo{sp}": s.f1mo[sp],
+                    f"s1mo{sp}": s.s1mo[sp], f"mo1_solved{sp}": _from_py(mo1_py[sp]),
+                    f"mo1{sp}": _from_py(fin["mo1"][sp]), f"mo_e1{sp}": _from_py(fin["mo_e1"][sp])})
+    np.savez(HERE / f"{tag}_seed{seed}.npz", **out)
+
+
+def main():
+    if not (REF / "pyhessref").is_dir():
+        raise SystemExit(f"reference not found at {REF}")
+    _install_stub_pyscf()
+    sys.path.insert(0, str(REF))
+    krylov_golden()
+    rhf_golden("rhf_nao24", seed=1)
+    uhf_golden(dict(nao=20, naux=70, nocc=(5, 4), natm=3, decay=6.0), "uhf_nao20", seed=2)
+    print("golden vectors written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

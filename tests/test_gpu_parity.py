@@ -1,0 +1,269 @@
+"""GPU parity: every libcphf entry point against the CPU oracle on the same seeded inputs.
+
+Bars: FP64 plugin responses and driver steps agree with the oracle to 1e-12 relative
+(max |diff| / max |ref|); FP64 solves to 1e-10 relative; the mixed-precision solve reaches
+max_j ||b - (I+A)x||_2 < 1e-8 and its U1 and Hessian agree with FP64 within 1e-7.
+"""
+
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_err
+from cphf_gb300 import Context, CphfError, KrylovNotConverged, synth
+from oracle import cphf, krylov, rijk, xc
+
+pytestmark = pytest.mark.gpu
+
+MEDIUM = dict(nao=96, naux=300, nocc=(12,), natm=8, decay=12.0)
+MEDIUM_U = dict(nao=80, naux=260, nocc=(11, 9), natm=6, decay=12.0)
+GRID_R = dict(nao=64, naux=200, nocc=(9,), natm=4, decay=10.0, grid=True, points=(700, 1300), window=20)
+GRID_U = dict(nao=60, naux=180, nocc=(8, 7), natm=4, decay=10.0, grid=True, points=(600, 1100), window=20)
+
+
+def make_ctx(s, precision="fp64", **cfg):
+    ctx = Context(precision=precision, **cfg)
+    ctx.set_cderi(s.cderi, s.scale_j, s.scale_k)
+    if s.grid is not None:
+        ctx.set_grid(s.grid.ao, s.grid.weights, s.grid.fxc, s.nspin, s.grid.atom_offsets)
+    if s.nspin == 1:
+        ctx.make_response_preparation(s.mo_coeff[0], s.mo_occ[0], s.mo_energy[0])
+    else:
+        ctx.make_response_preparation(s.mo_coeff, s.mo_occ, s.mo_energy)
+    return ctx
+
+
+def oracle_plugins(s):
+    mocc = [s.mo_coeff[t][:, :s.nocc[t]] for t in range(s.nspin)]
+    plugs = []
+    if s.nspin == 1:
+        plugs.append(lambda b: rijk.rhf_response_bra(s.cderi, s.mo_coeff[0], s.mo_occ[0], b, s.scale_j, s.scale_k))
+        if s.grid is not None:
+            g = s.grid
+            plugs.append(lambda b: xc.rks_response_bra(g.ao, g.weights, g.fxc, b, mocc[0]))
+    else:
+        plugs.append(lambda b: rijk.uhf_response_bra(s.cderi, s.mo_coeff, s.mo_occ, b, s.scale_j, s.scale_k))
+        if s.grid is not None:
+            g = s.grid
+            plugs.append(lambda b: xc.uks_response_bra(g.ao, g.weights, g.fxc, b, mocc))
+    return plugs
+
+
+def oracle_driver(s, **cfg):
+    if s.nspin == 1:
+        return cphf.RHF(s.mo_coeff[0], s.mo_occ[0], s.mo_energy[0], oracle_plugins(s), s.natm, config=cfg)
+    return cphf.UHF(s.mo_coeff, s.mo_occ, s.mo_energy, oracle_plugins(s), s.natm, config=cfg)
+
+
+@pytest.fixture(scope="module")
+def med():
+    s = synth.make_system(MEDIUM, seed=7)
+    return s, make_ctx(s)
+
+
+@pytest.mark.parametrize("dims,seed", [("rhf_nao24", 1), (MEDIUM, 7)])
+def test_rijk_response_bra_rhf(dims, seed):
+    s = synth.make_system(dims, seed=seed)
+    ctx = make_ctx(s)
+    bra = np.random.default_rng(seed).standard_normal((s.nao, s.nocc[0], 7))
+    got = ctx.get_response_bra(bra)
+    ref = rijk.rhf_response_bra(s.cderi, s.mo_coeff[0], s.mo_occ[0], bra, s.scale_j, s.scale_k)
+    assert rel_err(got, ref) < 1e-12
+
+
+def test_rijk_response_matches_reference_golden():
+    g = load_golden("rhf_nao24_seed1.npz")
+    ctx = Context()
+    ctx.set_cderi(g["cderi"], float(g["scale_j"]), float(g["scale_k"]))
+    ctx.make_response_preparation(g["mo_coeff"], g["mo_occ"], g["mo_energy"])
+    assert rel_err(ctx.get_response_bra(g["bra_probe"]), g["resp_probe"]) < 1e-12
+
+
+@pytest.mark.parametrize("sj,sk", [(1.0, 0.0), (0.0, 0.7), (1.3, 0.25)])
+def test_rijk_scales_and_j_or_k_only(sj, sk):
+    s = synth.make_system(MEDIUM, seed=8, scale_j=sj, scale_k=sk)
+    ctx = make_ctx(s)
+    bra = np.random.default_rng(2).standard_normal((s.nao, s.nocc[0], 3))
+    ref = rijk.rhf_response_bra(s.cderi, s.mo_coeff[0], s.mo_occ[0], bra, sj, sk)
+    assert rel_err(ctx.get_response_bra(bra), ref) < 1e-12
+
+
+def test_rijk_k_term_aux_chunking():
+    s = synth.make_system(MEDIUM, seed=9)
+    ctx = make_ctx(s, aux_chunk=37)   # ragged last chunk
+    bra = np.random.default_rng(3).standard_normal((s.nao, s.nocc[0], 5))
+    ref = rijk.rhf_response_bra(s.cderi, s.mo_coeff[0], s.mo_occ[0], bra, s.scale_j, s.scale_k)
+    assert rel_err(ctx.get_response_bra(bra), ref) < 1e-12
+
+
+def test_rijk_response_bra_uhf():
+    s = synth.make_system(MEDIUM_U, seed=4)
+    ctx = make_ctx(s)
+    rng = np.random.default_rng(4)
+    bra = [rng.standard_normal((s.nao, s.nocc[t], 6)) for t in range(2)]
+    got = ctx.get_response_bra(bra)
+    ref = rijk.uhf_response_bra(s.cderi, s.mo_coeff, s.mo_occ, bra, s.scale_j, s.scale_k)
+    for t in range(2):
+        assert rel_err(got[t], ref[t]) < 1e-12
+
+
+def test_xc_response_rks():
+    s = synth.make_system(GRID_R, seed=5)
+    ctx = make_ctx(s)
+    bra = np.random.default_rng(5).standard_normal((s.nao, s.nocc[0], 4))
+    g = s.grid
+    ref = xc.rks_response_bra(g.ao, g.weights, g.fxc, bra, s.mo_coeff[0][:, :s.nocc[0]])
+    assert rel_err(ctx.get_response_bra(bra, plugin="xc"), ref) < 1e-12
+    both = ref + rijk.rhf_response_bra(s.cderi, s.mo_coeff[0], s.mo_occ[0], bra, s.scale_j, s.scale_k)
+    assert rel_err(ctx.get_response_bra(bra), both) < 1e-12
+
+
+def test_xc_response_uks():
+    s = synth.make_system(GRID_U, seed=6)
+    ctx = make_ctx(s)
+    rng = np.random.default_rng(6)
+    bra = [rng.standard_normal((s.nao, s.nocc[t], 3)) for t in range(2)]
+    g = s.grid
+    ref = xc.uks_response_bra(g.ao, g.weights, g.fxc, bra, [s.mo_coeff[t][:, :s.nocc[t]] for t in range(2)])
+    got = ctx.get_response_bra(bra, plugin="xc")
+    for t in range(2):
+        assert rel_err(got[t], ref[t]) < 1e-12
+
+
+@pytest.mark.parametrize("dims", [MEDIUM, MEDIUM_U, GRID_R])
+def test_response_mo_and_dimless(dims):
+    s = synth.make_system(dims, seed=10)
+    ctx = make_ctx(s)
+    drv = oracle_driver(s)
+    rng = np.random.default_rng(10)
+    if s.nspin == 1:
+        mo1 = rng.standard_normal((s.nao, s.nocc[0], 4))
+        assert rel_err(ctx.response_mo(mo1), drv.response_mo(mo1)) < 1e-12
+        assert rel_err(ctx.response_dimless_cphf(mo1), drv.response_dimless_cphf(mo1)) < 1e-12
+    else:
+        mo1 = [rng.standard_normal((s.nao, s.nocc[t], 4)) for t in range(2)]
+        for a, b in zip(ctx.response_dimless_cphf(mo1), drv.response_dimless_cphf(mo1)):
+            assert rel_err(a, b) < 1e-12
+
+
+def test_solve_finalize_hess_rhf_golden():
+    """The whole CPHF chain against the reference Python driver's golden vectors."""
+    g = load_golden("rhf_nao24_seed1.npz")
+    ctx = Context(cphf_tol=1e-10, cphf_max_cycle=30)
+    ctx.set_cderi(g["cderi"], float(g["scale_j"]), float(g["scale_k"]))
+    ctx.make_response_preparation(g["mo_coeff"], g["mo_occ"], g["mo_energy"])
+    mo1 = ctx.solve_dimless_cphf(g["rhs"])
+    nocc = int((g["mo_occ"] > 0).sum())
+    assert rel_err(mo1[nocc:], g["mo1_solved"][nocc:]) < 1e-8
+    mo1f, mo_e1 = ctx.finalize_cphf(g["f1mo"], g["s1mo"], g["mo1_solved"])
+    assert rel_err(mo1f, g["mo1"]) < 1e-11
+    assert rel_err(mo_e1, g["mo_e1"]) < 1e-11
+    de = ctx.get_cphf_hess(g["f1mo"], g["s1mo"], g["mo1"], g["mo_e1"])
+    assert rel_err(de, g["de_cphf"]) < 1e-12
+
+
+@pytest.mark.parametrize("dims", [MEDIUM, MEDIUM_U, GRID_R, GRID_U])
+def test_solve_dimless_cphf_fp64_matches_oracle(dims):
+    s = synth.make_system(dims, seed=12)
+    ctx = make_ctx(s, cphf_tol=1e-10)
+    drv = oracle_driver(s, cphf_tol=1e-10)
+    rhs = s.rhs[0] if s.nspin == 1 else s.rhs
+    got = ctx.solve_dimless_cphf(rhs)
+    ref = drv.solve_dimless_cphf(rhs)
+    st = ctx.last_stats
+    assert st["aop_calls"] == drv.krylov_stats["aop_calls"]
+    if s.nspin == 1:
+        got, ref = [got], [ref]
+    for a, b in zip(got, ref):
+        assert rel_err(a, b) < 1e-10
+    f1 = s.f1mo[0] if s.nspin == 1 else s.f1mo
+    s1 = s.s1mo[0] if s.nspin == 1 else s.s1mo
+    m1 = got[0] if s.nspin == 1 else got
+    mf, me = ctx.finalize_cphf(f1, s1, m1)
+    rf, re_ = drv.finalize_cphf(f1, s1, m1)
+    if s.nspin == 1:
+        mf, me, rf, re_ = [mf], [me], [rf], [re_]
+    for a, b in zip(mf, rf):
+        assert rel_err(a, b) < 1e-11
+    for a, b in zip(me, re_):
+        assert rel_err(a, b) < 1e-11
+    de = ctx.get_cphf_hess(f1, s1, mf[0] if s.nspin == 1 else mf, me[0] if s.nspin == 1 else me)
+    ref_de = drv.get_cphf_hess(f1, s1, rf[0] if s.nspin == 1 else rf, re_[0] if s.nspin == 1 else re_)
+    assert rel_err(de, ref_de) < 1e-11
+
+
+@pytest.mark.parametrize("dims", [MEDIUM, GRID_U])
+def test_mixed_precision_solve(dims):
+    s = synth.make_system(dims, seed=13)
+    rhs = s.rhs[0] if s.nspin == 1 else s.rhs
+    c64 = make_ctx(s, cphf_tol=1e-10, cphf_lindep=1e-20)
+    x64 = c64.solve_dimless_cphf(rhs)
+    cmx = make_ctx(s, precision="mixed")
+    xmx = cmx.solve_dimless_cphf(rhs)
+    st = cmx.last_stats
+    assert st["residual_max"] < 1e-8
+    assert st["refine_steps"] >= 1 and st["lowp_matvec_columns"] > 0
+    if s.nspin == 1:
+        x64, xmx = [x64], [xmx]
+    for a, b in zip(xmx, x64):
+        assert np.abs(a - b).max() < 1e-7
+    f1 = s.f1mo[0] if s.nspin == 1 else s.f1mo
+    s1 = s.s1mo[0] if s.nspin == 1 else s.s1mo
+    h = []
+    for ctx, x in [(c64, x64), (cmx, xmx)]:
+        m1, me = ctx.finalize_cphf(f1, s1, x[0] if s.nspin == 1 else x)
+        h.append(ctx.get_cphf_hess(f1, s1, m1, me))
+    assert np.abs(h[0] - h[1]).max() < 1e-7
+
+
+def test_gpu_krylov_reference_fixture():
+    """tests/test_krylov_block.rs:7-97 through the device solver (dense operator on the GPU)."""
+    z = load_golden("krylov_fixture.npz")
+    A, b, x_ref = z["A"], z["b"].T.copy(), z["x_ref"].T.copy()
+    ctx = Context()
+    x = ctx.krylov_block(A, b, None, 1e-10, 30, 6, 1e-13)
+    assert np.allclose(x, x_ref, rtol=1e-6, atol=1e-8)
+    assert np.abs(x + A @ x - b).max() < 1e-6
+    assert ctx.last_stats["aop_calls"] == int(z["calls_ms6"])
+    xr = ctx.krylov_block(A, b, None, 1e-10, 60, 3, 1e-13)
+    assert ctx.last_stats["restarts"] >= 1
+    assert np.allclose(xr, x_ref, rtol=1e-5, atol=1e-6)
+    ox = krylov.krylov_block(lambda v: A @ v, b, None, 1e-10, 60, 3, 1e-13)
+    assert np.abs(xr - ox).max() < 1e-10
+    with pytest.raises(KrylovNotConverged):
+        ctx.krylov_block(A, b, None, 1e-10, 2, 14, 1e-13)
+
+
+def test_gpu_krylov_host_callback_operator():
+    z = load_golden("krylov_fixture.npz")
+    A, b = z["A"], z["b"].T.copy()
+    ctx = Context()
+    x = ctx.krylov_block(lambda v: A @ v, b, None, 1e-10, 30, 6, 1e-13)
+    ox = krylov.krylov_block(lambda v: A @ v, b, None, 1e-10, 30, 6, 1e-13)
+    assert np.abs(x - ox).max() < 1e-10
+
+
+def test_errors_are_status_codes(med):
+    s, ctx = med
+    bad = s.rhs[0].copy()
+    bad[3, 1, 0, 0] = np.nan
+    with pytest.raises(CphfError) as e:
+        ctx.solve_dimless_cphf(bad)
+    assert e.value.status == 3
+    with pytest.raises(KrylovNotConverged):
+        c2 = make_ctx(s, cphf_max_cycle=1)
+        c2.solve_dimless_cphf(s.rhs[0])
+    with pytest.raises(CphfError) as e:
+        Context().get_response_bra(np.zeros((4, 2, 1)))
+    assert e.value.status in (7, 8)
+
+
+def test_empty_and_single_column(med):
+    s, ctx = med
+    one = ctx.get_response_bra(np.ones((s.nao, s.nocc[0], 1)))
+    ref = rijk.rhf_response_bra(s.cderi, s.mo_coeff[0], s.mo_occ[0], np.ones((s.nao, s.nocc[0], 1)),
+                                s.scale_j, s.scale_k)
+    assert rel_err(one, ref) < 1e-12
+    zero = ctx.get_response_bra(np.zeros((s.nao, s.nocc[0], 0)))
+    assert zero.shape == (s.nao, s.nocc[0], 0)
+    x = ctx.solve_dimless_cphf(np.zeros((s.nao, s.nocc[0], 2)))
+    assert np.all(x == 0.0)
