@@ -1,0 +1,370 @@
+#!/usr/bin/env python3
+"""Benchmark: time to a converged CPHF solve (max_j ||b - (I+A)x||_2 < 1e-8) on one GB300.
+
+A step is one full ``solve_dimless_cphf`` of the workload (default ``rhf_nao600``:
+nao=600, naux=2000, nocc=60, 180 right-hand sides, RHF with RI-J/RI-K response) through
+libcphf.  The timed arm is the mixed-precision solve (split-FP16 tensor-core operator
+inside FP64 defect correction); the plain FP64 GPU solve of the same system is timed once
+beside it, and both solutions are verified with the FP64 operator outside the timed region.
+
+``--impl reference`` times the reference algorithm on the host CPU instead (the numpy
+port in ``oracle/``, all cores), on the same workload and metric.
+
+Prints one JSON line (rank 0).  Multi-GPU runs are independent replicas (the path is not
+sharded): one process per GPU via torchrun, max time over ranks.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "rstsr-showcase-hessian_gb300"))
+sys.path.insert(0, str(ROOT))
+
+METRIC = "time to converged CPHF (||r||<1e-8): mixed+learned vs plain FP64, same GB300"
+WORKLOAD_DESC = {
+    "rhf_nao600": "RHF CPHF, RI-JK response: nao=600 naux=2000 nocc=60 nvir=540 nrhs=180 (60 atoms)",
+    "rhf_nao24": "RHF CPHF, RI-JK response: nao=24 naux=84 nocc=5 nrhs=12 (4 atoms)",
+    "rhf_nao300": "RHF CPHF, RI-JK response: nao=300 naux=1000 nocc=30 nrhs=90 (30 atoms)",
+    "rks_nao600": "RKS CPKS, RI-JK + LDA XC response on ~660k grid points: nao=600 naux=2000 nocc=60 nrhs=180",
+    "uks_nao800": "UKS CPKS, RI-JK + LDA XC: nao=800 naux=2700 nocc=80/78 nrhs=240",
+    "rhf_nao1200": "RHF CPHF, RI-JK response: nao=1200 naux=4000 nocc=120 nrhs=360",
+}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=2)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["cphf", "reference"], default="cphf")
+    p.add_argument("--workload", default="rhf_nao600")
+    p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison solve")
+    p.add_argument("--cpu-sample", type=int, default=12, help="RHS columns of the CPU baseline sample")
+    return p.parse_args()
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if args.impl == "cphf" else "gloo"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- CPU (oracle) timing
+def cpu_oracle_estimate(s, ncols):
+    """Reference algorithm on the host (oracle port): a real Krylov solve of `ncols` RHS
+    columns with the full-size operator gives the operator-call count; single matvecs at
+    ncols and 2*ncols give the per-call cost model t0 + t1*nb, extrapolated to all columns."""
+    from oracle import cphf as ocphf
+    from oracle import rijk as orijk
+    C, occ, e = s.mo_coeff[0], s.mo_occ[0], s.mo_energy[0]
+    plug = lambda bra: orijk.rhf_response_bra(s.cderi, C, occ, bra, s.scale_j, s.scale_k)  # noqa: E731
+    drv = ocphf.RHF(C, occ, e, [plug], s.natm)
+    nrhs = s.rhs[0].shape[2] * s.rhs[0].shape[3]
+    rhs = s.rhs[0].reshape(s.nao, s.nocc[0], nrhs, order="F")
+    x1 = rhs[:, :, :ncols]
+    x2 = rhs[:, :, :2 * ncols]
+    t = time.perf_counter(); drv.response_dimless_cphf(x1); t1 = time.perf_counter() - t
+    t = time.perf_counter(); drv.response_dimless_cphf(x2); t2 = time.perf_counter() - t
+    slope = max((t2 - t1) / ncols, 1e-12)
+    base = max(t1 - slope * ncols, 0.0)
+    t = time.perf_counter()
+    drv.solve_dimless_cphf(x1)
+    t_solve = time.perf_counter() - t
+    calls = drv.krylov_stats["aop_calls"]
+    cols_per_call = drv.krylov_stats["aop_columns"] / max(calls, 1) / ncols
+    est = calls * (base + slope * nrhs * cols_per_call)
+    cores = os.cpu_count()
+    return dict(value=est, unit="s", cores=cores, kind="port",
+                sample=(f"oracle (numpy/OpenBLAS, {cores} threads) CPHF solve of {ncols} of {nrhs} RHS "
+                        f"({calls} operator calls, {t_solve:.1f} s) plus matvecs at {ncols} and {2 * ncols} "
+                        f"columns ({t1:.2f} s, {t2:.2f} s); value = calls x (t0 + t1*{nrhs}) extrapolated"),
+                calls=calls, matvec_s_per_col=slope, matvec_fixed_s=base)
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from cphf_gb300 import synth
+    s = synth.make_system(args.workload, seed=args.seed)
+    steps = []
+    for _ in range(args.warmup + args.steps):
+        steps.append(cpu_oracle_estimate(s, args.cpu_sample))
+    timed = steps[args.warmup:]
+    value = statistics.median([x["value"] for x in timed])
+    cb = dict(timed[-1])
+    cb["value"] = value
+    line = dict(metric=METRIC, value=value, unit="s", n_gpus=args.gpus, steps=args.steps, warmup=args.warmup,
+                ms_per_step=value * 1e3, higher_is_better=False, scaling="weak", vs_baseline=None, dtype="f64",
+                data=f"synthetic (seeded generator, {args.workload}, seed {args.seed})",
+                config=dict(workload=args.workload, description=WORKLOAD_DESC.get(args.workload, args.workload)),
+                impl="reference",
+                cpu_baseline={k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                e2e=dict(value=value, unit="s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU arm
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return dict(sm_mhz=None, sm_max_mhz=None, reasons=["nvidia-smi unavailable"])
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        sm, mx, reasons = [], None, set()
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return dict(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=mx, reasons=sorted(reasons),
+                    samples=len(sm))
+
+
+def measure_fp64_peak():
+    """cuBLAS FP64 GEMM rate on this GPU (torch.matmul), the denominator for FP64-pipe kernels."""
+    import torch
+    n = 8192
+    a = torch.randn(n, n, device="cuda", dtype=torch.float64)
+    b = torch.randn(n, n, device="cuda", dtype=torch.float64)
+    a @ b
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(); a @ b; e1.record(); torch.cuda.synchronize()
+    return 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def fcol(t):
+    """col-major [nmo, nocc, 3, natm] view of a torch tensor stored with reversed C-order dims."""
+    return t.permute(*reversed(range(t.dim())))
+
+
+def run_gpu(args, world, rank, local):
+    import torch
+    import cphf_gb300
+    from cphf_gb300 import synth
+
+    torch.cuda.set_device(local)
+    cphf_gb300.build()
+    s = synth.make_system(args.workload, seed=args.seed)
+    nspin = s.nspin
+    rhs_h = s.rhs if nspin == 2 else [s.rhs[0]]
+
+    def make_ctx(precision, **cfg):
+        ctx = cphf_gb300.Context(precision=precision, device=local, **cfg)
+        ctx.set_cderi(s.cderi, s.scale_j, s.scale_k)
+        if s.grid is not None:
+            ctx.set_grid(s.grid.ao, s.grid.weights, s.grid.fxc, nspin, s.grid.atom_offsets)
+        if nspin == 1:
+            ctx.make_response_preparation(s.mo_coeff[0], s.mo_occ[0], s.mo_energy[0])
+        else:
+            ctx.make_response_preparation(s.mo_coeff, s.mo_occ, s.mo_energy)
+        return ctx
+
+    mixed = make_ctx("mixed", verify_residual=0)
+    # device-resident inputs and outputs (F-contiguous views of C-ordered tensors)
+    rhs_d = [fcol(torch.from_numpy(np.ascontiguousarray(r.transpose(3, 2, 1, 0))).cuda()) for r in rhs_h]
+    out_d = [fcol(torch.empty(tuple(reversed(r.shape)), dtype=torch.float64, device="cuda")) for r in rhs_h]
+    arg = (lambda v: v if nspin == 2 else v[0])
+    stream = torch.cuda.ExternalStream(mixed.stream)
+
+    for _ in range(args.warmup):
+        mixed.solve_dimless_cphf(arg(rhs_d), out=arg(out_d))
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    mixed.profile(True)
+    l0 = mixed.kernel_launches
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    stats = []
+    for _ in range(args.steps):
+        mixed.solve_dimless_cphf(arg(rhs_d), out=arg(out_d))
+        stats.append(mixed.last_stats)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    launches = mixed.kernel_launches - l0
+    prof = mixed.profile_report()
+    mixed.profile(False)
+    clk = clocks.stop()
+    t_step = ev0.elapsed_time(ev1) * 1e-3 / args.steps
+    t_step = max_over_ranks(world, t_step)
+
+    # end to end through the C ABI with pinned host buffers (copies inside the timed region)
+    rhs_p = [torch.from_numpy(np.ascontiguousarray(r.transpose(3, 2, 1, 0))).pin_memory() for r in rhs_h]
+    out_p = [torch.empty(tuple(reversed(r.shape)), dtype=torch.float64).pin_memory() for r in rhs_h]
+    rhs_pf = [fcol(t) for t in rhs_p]
+    out_pf = [fcol(t) for t in out_p]
+    h2d = sum(r.nbytes for r in rhs_h)
+    d2h = h2d
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        mixed.solve_dimless_cphf(arg(rhs_pf), out=arg(out_pf))
+    t_e2e = max_over_ranks(world, (time.perf_counter() - t) / args.steps)
+    x_mixed = [o.numpy().transpose(3, 2, 1, 0).copy(order="F") for o in out_p]
+
+    # plain FP64 solve of the same system (the reference's arithmetic), timed once
+    fp64 = make_ctx("fp64", cphf_tol=1e-9)
+    fp64_res = None
+    if not args.no_fp64:
+        t = time.perf_counter()
+        x64 = fp64.solve_dimless_cphf(arg(rhs_h))
+        t_fp64 = time.perf_counter() - t
+        st64 = fp64.last_stats
+        x64 = x64 if nspin == 2 else [x64]
+
+    # verification outside the timed regions: FP64 residuals and Hessian blocks
+    def residual(x):
+        y = fp64.response_dimless_cphf(arg(x))
+        y = y if nspin == 2 else [y]
+        return max(float(np.linalg.norm((b - xx - yy).reshape(-1, b.shape[2] * b.shape[3], order="F"),
+                                        axis=0).max()) for b, xx, yy in zip(rhs_h, x, y))
+
+    res_mixed = residual(x_mixed)
+    hess_diff = None
+    if not args.no_fp64:
+        fp64_res = residual(x64)
+        f1 = s.f1mo if nspin == 2 else s.f1mo[0]
+        s1 = s.s1mo if nspin == 2 else s.s1mo[0]
+        h = []
+        for x in (x_mixed, x64):
+            m1, me = fp64.finalize_cphf(f1, s1, arg(x))
+            h.append(fp64.get_cphf_hess(f1, s1, m1, me))
+        hess_diff = float(np.abs(h[0] - h[1]).max())
+
+    # roofline of the dominant kernel class in the timed region
+    hbm, bf16, peak_src = load_peaks()
+    dom_name, dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    if dom_name == "gemm_fp64_simt":
+        peak = measure_fp64_peak()
+        roof = dict(bound="tensor", achieved=dom["flops"] / dom["ms"] / 1e9, peak=peak, unit="TFLOP/s",
+                    peak_source="in-run cuBLAS FP64 GEMM 8192^3 (FP64 has no entry in MEASURED_PEAKS.json)")
+    elif dom_name == "kterm_tcgen05_f16x3":
+        roof = dict(bound="tensor", achieved=dom["flops"] / dom["ms"] / 1e9, peak=bf16, unit="TFLOP/s",
+                    peak_source=f"{peak_src} bf16 dense (FP16 runs at the same rate); achieved counts "
+                                "algorithmic FLOPs, the tensor pipe executes 3 split products")
+    else:
+        roof = dict(bound="tensor", achieved=dom["flops"] / dom["ms"] / 1e9, peak=bf16, unit="TFLOP/s",
+                    peak_source=peak_src)
+    roof.update(kernel=dom_name, frac=roof["achieved"] / roof["peak"], traffic=None,
+                launches=dom["launches"], avg_launch_ms=dom["ms"] / dom["launches"],
+                share_of_step=dom["ms"] * 1e-3 / (t_step * args.steps))
+
+    cpu = cpu_oracle_estimate(s, args.cpu_sample) if rank == 0 and nspin == 1 else None
+    st = stats[-1]
+    line = dict(
+        metric=METRIC, value=t_step, unit="s", n_gpus=args.gpus, steps=args.steps, warmup=args.warmup,
+        ms_per_step=t_step * 1e3, higher_is_better=False, scaling="weak", vs_baseline=None,
+        dtype="f16x3 tensor-core operator / f32 / f64 defect correction",
+        data=f"synthetic (seeded generator, {args.workload}, seed {args.seed})",
+        config=dict(workload=args.workload, description=WORKLOAD_DESC.get(args.workload, args.workload),
+                    precision="mixed", learned_guess=False, parallelism="replicas" if world > 1 else "single GPU",
+                    l2="inputs larger than L2 (dense cderi FP64 %.1f GB)" % (s.nao ** 2 * s.naux * 8 / 1e9)),
+        fp64_plain=None if args.no_fp64 else dict(value=t_fp64, unit="s", aop_calls=st64["aop_calls"],
+                                                  cycles=st64["cycles"], tol=1e-9),
+        speedup_vs_fp64_plain=None if args.no_fp64 else t_fp64 / t_step,
+        residual=dict(mixed_verified=res_mixed, fp64_plain_verified=fp64_res, target=1e-8),
+        hessian_max_abs_diff_vs_fp64=hess_diff,
+        solve_stats=dict(refine_steps=st["refine_steps"], fp64_matvec_columns=st["fp64_matvec_columns"],
+                         lowp_matvec_columns=st["lowp_matvec_columns"], cycles=st["cycles"],
+                         tensor_cores=mixed.tensor_cores_active),
+        kernel_classes={k: dict(launches=v["launches"], ms=round(v["ms"], 3),
+                                tflops=round(v["flops"] / max(v["ms"], 1e-9) / 1e9, 2)) for k, v in prof.items()},
+        e2e=dict(value=t_e2e, unit="s", h2d_bytes_per_step=h2d, d2h_bytes_per_step=d2h),
+        gpu_launches=int(launches),
+        roofline=roof,
+        cpu_baseline=None if cpu is None else {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        clocks=clk,
+    )
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -63,6 +63,9 @@ typedef struct cphf_config {
   int32_t use_learned_guess; /* use the MLP initial guess / preconditioner if weights are set (default 0) */
   int32_t verbose;           /* print per-cycle diagnostics like krylov_block.rs:148-151 (default 0) */
   int64_t aux_chunk;         /* aux functions per K-term chunk (default 0 = automatic) */
+  int32_t tensor_cores;      /* mixed: 1 = tcgen05 split-FP16 K term (default), 0 = FP32 CUDA cores */
+  int32_t verify_residual;   /* mixed: recompute the final residual with the FP64 operator (default 1) */
+  int32_t fp64_every_step;   /* mixed: FP64 residual after every correction, not only the first (default 0) */
 } cphf_config;
 
 /* Solver statistics (the reference reports them by println!, krylov_block.rs:148-151, 175). */
@@ -100,6 +103,22 @@ cphf_status cphf_ctx_synchronize(cphf_ctx* ctx);
 int64_t cphf_ctx_device_bytes(const cphf_ctx* ctx);   /* device memory held by the context */
 /* Number of kernels this context launched so far (launch counter, for benchmarks). */
 int64_t cphf_ctx_kernel_launches(const cphf_ctx* ctx);
+/* 1 when the split-precision operator runs its K term on the tensor cores (tcgen05). */
+int32_t cphf_ctx_tensor_cores_active(const cphf_ctx* ctx);
+
+/* Per-kernel-class timing with CUDA events (replaces the reference's wall-clock timing
+ * vectors, src/hessian/rscf.rs:33).  Enabling clears the records. */
+typedef struct cphf_prof_entry {
+  char name[32];
+  int64_t launches;
+  double ms;       /* summed event time */
+  double max_ms;   /* longest single launch */
+  double flops;    /* algorithmic FLOPs of the recorded launches */
+  double bytes;    /* algorithmic bytes of the recorded launches */
+} cphf_prof_entry;
+cphf_status cphf_ctx_profile(cphf_ctx* ctx, int32_t enable);
+/* Fills up to `max` entries (one per kernel class with records); returns the count, or -1. */
+int32_t cphf_ctx_profile_report(cphf_ctx* ctx, cphf_prof_entry* out, int32_t max);
 
 /* ---- RI-JK plugin ---------------------------------------------------------------------- */
 /* RHessRIJK::new_with_cderi (src/ri_jk/hess_r.rs:1774-1794) / UHessRIJK:
@@ -144,6 +163,10 @@ cphf_status cphf_response_mo(cphf_ctx* ctx, const double* const* mo1, int64_t np
 /* response_dimless_cphf (rscf.rs:237-263, uscf.rs:230-265). */
 cphf_status cphf_response_dimless(cphf_ctx* ctx, const double* const* mo1, int64_t nprop,
                                   double* const* resp);
+/* The same operator in the split-precision arithmetic of the mixed solve (FP32 / tensor cores);
+ * valid after cphf_prepare on a context configured with CPHF_PRECISION_MIXED. */
+cphf_status cphf_response_dimless_lowp(cphf_ctx* ctx, const double* const* mo1, int64_t nprop,
+                                       double* const* resp);
 /* solve_dimless_cphf (rscf.rs:278-300, uscf.rs:278-341): rhs[s], mo1[s] [nmo, nocc_s, nprop];
  * x0 may be NULL.  FP64: krylov_block with the fused dimensionless operator.
  * MIXED: the same solver on the split-precision operator inside FP64 defect correction. */
@@ -180,8 +203,28 @@ cphf_status cphf_copy(cphf_ctx* ctx, void* dst, const void* src, int64_t bytes);
 
 /* ---- learned initial guess / preconditioner (no counterpart in the reference) ------------ */
 /* Per-(i,a)-pair MLP 3 -> 64 -> 64 -> 2 (GELU), FP32 weights packed as
- * W1[64,3] b1[64] W2[64,64] b2[64] W3[2,64] b3[2] (row-major per matrix). */
+ * W1[64,3] b1[64] W2[64,64] b2[64] W3[2,64] b3[2] (row-major per matrix), 4546 floats.
+ * Sample features [n, 3] (row-major): gap e_a - e_i, dimensionless RHS entry b, (ia|ia).
+ * Outputs [n, 2]: o1 (initial guess x0 = b (1 + o1)), o2 (effective diagonal d of the
+ * dimensionless operator; preconditioner 1 / (1 + d)).  With use_learned_guess set, the
+ * solve starts from the guess and left-preconditions the Krylov iteration; the unmodified
+ * operator still defines convergence (mixed: the FP64 residual), so the answer is unchanged. */
 cphf_status cphf_mlp_set_weights(cphf_ctx* ctx, const float* weights, int64_t nweights);
+cphf_status cphf_mlp_get_weights(cphf_ctx* ctx, float* weights, int64_t nweights);
+/* Features of every (vir a, occ i, column r) sample of rhs[s] [nmo, nocc_s, nprop]
+ * (order: spin, then r slowest, then i, a fastest); *n_out receives the count, `feat` may be
+ * NULL to query it. */
+cphf_status cphf_mlp_features(cphf_ctx* ctx, const double* const* rhs, int64_t nprop, float* feat,
+                              int64_t cap, int64_t* n_out);
+/* Network outputs; bf16 != 0 selects the BF16 inference kernel, else FP32. */
+cphf_status cphf_mlp_forward(cphf_ctx* ctx, const float* feat, int64_t n, float* out, int32_t bf16);
+/* Mean loss (b (1 + o1) - x*)^2 + (o2 - d*)^2 and its gradient [4546]; target [n, 2] = (x*, d*). */
+cphf_status cphf_mlp_loss_grad(cphf_ctx* ctx, const float* feat, const float* target, int64_t n,
+                               float* loss, float* grad);
+/* Adam training on the GPU: `epochs` passes over shuffled minibatches; history[epochs] gets
+ * the mean minibatch loss per epoch (may be NULL). */
+cphf_status cphf_mlp_train(cphf_ctx* ctx, const float* feat, const float* target, int64_t n,
+                           int64_t epochs, int64_t batch, float lr, uint64_t seed, float* history);
 
 #ifdef __cplusplus
 }

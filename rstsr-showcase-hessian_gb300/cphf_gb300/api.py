@@ -31,10 +31,25 @@ EXPORTS = [
     "cphf_status_string", "cphf_last_error", "cphf_ctx_stream", "cphf_ctx_synchronize",
     "cphf_ctx_device_bytes", "cphf_ctx_kernel_launches", "cphf_rijk_set_cderi", "cphf_xc_set_grid",
     "cphf_set_nao", "cphf_prepare", "cphf_response_bra", "cphf_plugin_response_bra",
-    "cphf_response_mo", "cphf_response_dimless", "cphf_solve_dimless_cphf", "cphf_finalize_cphf",
+    "cphf_response_mo", "cphf_response_dimless", "cphf_response_dimless_lowp", "cphf_solve_dimless_cphf",
+    "cphf_finalize_cphf",
     "cphf_get_cphf_hess", "cphf_krylov_block", "cphf_dense_op_create", "cphf_dense_op_apply",
-    "cphf_dense_op_destroy", "cphf_copy", "cphf_mlp_set_weights",
+    "cphf_dense_op_destroy", "cphf_copy", "cphf_mlp_set_weights", "cphf_ctx_tensor_cores_active",
+    "cphf_ctx_profile", "cphf_ctx_profile_report", "cphf_mlp_get_weights", "cphf_mlp_features",
+    "cphf_mlp_forward", "cphf_mlp_loss_grad", "cphf_mlp_train",
 ]
+MLP_NWEIGHTS = 4546
+
+
+class ProfEntry(ctypes.Structure):
+    _fields_ = [
+        ("name", ctypes.c_char * 32),
+        ("launches", ctypes.c_int64),
+        ("ms", ctypes.c_double),
+        ("max_ms", ctypes.c_double),
+        ("flops", ctypes.c_double),
+        ("bytes", ctypes.c_double),
+    ]
 
 
 class Config(ctypes.Structure):
@@ -52,6 +67,9 @@ class Config(ctypes.Structure):
         ("use_learned_guess", ctypes.c_int32),
         ("verbose", ctypes.c_int32),
         ("aux_chunk", ctypes.c_int64),
+        ("tensor_cores", ctypes.c_int32),
+        ("verify_residual", ctypes.c_int32),
+        ("fp64_every_step", ctypes.c_int32),
     ]
 
 
@@ -116,6 +134,7 @@ def load_library():
         "cphf_plugin_response_bra": ([vp, i32, pp, i64, pp], i32),
         "cphf_response_mo": ([vp, pp, i64, pp], i32),
         "cphf_response_dimless": ([vp, pp, i64, pp], i32),
+        "cphf_response_dimless_lowp": ([vp, pp, i64, pp], i32),
         "cphf_solve_dimless_cphf": ([vp, pp, i64, pp, pp, ctypes.POINTER(Stats)], i32),
         "cphf_finalize_cphf": ([vp, pp, pp, i64, pp, pp], i32),
         "cphf_get_cphf_hess": ([vp, pp, pp, pp, pp, i64, vp], i32),
@@ -125,6 +144,14 @@ def load_library():
         "cphf_dense_op_destroy": ([vp], i32),
         "cphf_copy": ([vp, vp, vp, i64], i32),
         "cphf_mlp_set_weights": ([vp, vp, i64], i32),
+        "cphf_ctx_tensor_cores_active": ([vp], i32),
+        "cphf_ctx_profile": ([vp, i32], i32),
+        "cphf_ctx_profile_report": ([vp, ctypes.POINTER(ProfEntry), i32], i32),
+        "cphf_mlp_get_weights": ([vp, vp, i64], i32),
+        "cphf_mlp_features": ([vp, pp, i64, vp, i64, ctypes.POINTER(i64)], i32),
+        "cphf_mlp_forward": ([vp, vp, i64, vp, i32], i32),
+        "cphf_mlp_loss_grad": ([vp, vp, vp, i64, ctypes.POINTER(ctypes.c_float), vp], i32),
+        "cphf_mlp_train": ([vp, vp, vp, i64, i64, i64, ctypes.c_float, ctypes.c_uint64, vp], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -174,6 +201,10 @@ def _is_fcontig(t):
             return False
         expect *= size
     return True
+
+
+def _shape(a):
+    return tuple(a.shape) if hasattr(a, "shape") else np.shape(a)
 
 
 def _nprop(shape):
@@ -250,6 +281,23 @@ class Context:
     def synchronize(self):
         self._check(self.lib.cphf_ctx_synchronize(self.h))
 
+    @property
+    def tensor_cores_active(self):
+        return bool(self.lib.cphf_ctx_tensor_cores_active(self.h))
+
+    def profile(self, enable=True):
+        """Start (clearing old records) or stop per-kernel-class CUDA-event timing."""
+        self._check(self.lib.cphf_ctx_profile(self.h, 1 if enable else 0))
+
+    def profile_report(self):
+        """``{class: {launches, ms, max_ms, flops, bytes}}`` of the recorded launches."""
+        buf = (ProfEntry * 8)()
+        n = self.lib.cphf_ctx_profile_report(self.h, buf, 8)
+        if n < 0:
+            self._check(ERR_CUDA)
+        return {buf[i].name.decode(): dict(launches=buf[i].launches, ms=buf[i].ms, max_ms=buf[i].max_ms,
+                                           flops=buf[i].flops, bytes=buf[i].bytes) for i in range(n)}
+
     # -- plugins ---------------------------------------------------------------------------
     def set_cderi(self, cderi, scale_j=1.0, scale_k=1.0, nao=None):
         """``RHessRIJK::new_with_cderi`` (src/ri_jk/hess_r.rs:1774-1794); cderi ``[nao_tp, naux]``."""
@@ -305,7 +353,7 @@ class Context:
 
     def _call_spin(self, fn, x, out_rows, extra=()):
         xs, uhf = self._spins(x)
-        shapes = [np.shape(v) for v in xs]
+        shapes = [_shape(v) for v in xs]
         nprop = _nprop(shapes[0])
         outs = [np.zeros((out_rows(s),) + tuple(shapes[s][1:]), order="F") for s in range(len(xs))]
         k = _Keep()
@@ -325,12 +373,16 @@ class Context:
     def response_dimless_cphf(self, mo1):
         return self._call_spin(self.lib.cphf_response_dimless, mo1, lambda s: self.nmo)
 
+    def response_dimless_cphf_lowp(self, mo1):
+        """The dimensionless operator in the split-precision arithmetic of the mixed solve."""
+        return self._call_spin(self.lib.cphf_response_dimless_lowp, mo1, lambda s: self.nmo)
+
     def solve_dimless_cphf(self, rhs, x0=None, out=None):
         """``solve_dimless_cphf``; statistics of the solve go to ``self.last_stats``."""
         xs, uhf = self._spins(rhs)
-        nprop = _nprop(np.shape(xs[0]))
+        nprop = _nprop(_shape(xs[0]))
         if out is None:
-            out = [np.zeros(np.shape(v), order="F") for v in xs]
+            out = [np.zeros(_shape(v), order="F") for v in xs]
         else:
             out = list(out) if uhf else [out]
         k = _Keep()
@@ -349,9 +401,9 @@ class Context:
         f1, uhf = self._spins(f1mo)
         s1, _ = self._spins(s1mo)
         m1, _ = self._spins(mo1)
-        natm = int(np.prod(np.shape(f1[0])[2:])) // 3
+        natm = int(np.prod(_shape(f1[0])[2:])) // 3
         m1 = [np.array(v, order="F", dtype=np.float64, copy=True) for v in m1]
-        e1 = [np.zeros((self.nocc[s], self.nocc[s]) + tuple(np.shape(f1[s])[2:]), order="F")
+        e1 = [np.zeros((self.nocc[s], self.nocc[s]) + tuple(_shape(f1[s])[2:]), order="F")
               for s in range(len(f1))]
         k = _Keep()
         self._check(self.lib.cphf_finalize_cphf(self.h, k.ptrs(f1), k.ptrs(s1), natm, k.ptrs(m1), k.ptrs(e1)))
@@ -363,7 +415,7 @@ class Context:
         s1, _ = self._spins(s1mo)
         m1, _ = self._spins(mo1)
         e1, _ = self._spins(mo_e1)
-        natm = int(np.prod(np.shape(f1[0])[2:])) // 3
+        natm = int(np.prod(_shape(f1[0])[2:])) // 3
         de = np.zeros((3, 3, natm, natm), order="F")
         k = _Keep()
         self._check(self.lib.cphf_get_cphf_hess(self.h, k.ptrs(f1), k.ptrs(s1), k.ptrs(m1), k.ptrs(e1), natm,
@@ -414,6 +466,51 @@ class Context:
         self._check(status)
         return x
 
+    # -- learned initial guess / preconditioner ---------------------------------------------
     def set_mlp_weights(self, weights):
         w = np.ascontiguousarray(weights, dtype=np.float32)
         self._check(self.lib.cphf_mlp_set_weights(self.h, ctypes.c_void_p(w.ctypes.data), w.size))
+
+    def mlp_weights(self):
+        w = np.zeros(MLP_NWEIGHTS, dtype=np.float32)
+        self._check(self.lib.cphf_mlp_get_weights(self.h, ctypes.c_void_p(w.ctypes.data), w.size))
+        return w
+
+    def mlp_features(self, rhs):
+        """Features [n, 3] (gap, b, (ia|ia)) of every vir-occ sample of ``rhs``."""
+        xs, _ = self._spins(rhs)
+        nprop = _nprop(_shape(xs[0]))
+        k = _Keep()
+        n = ctypes.c_int64()
+        p = k.ptrs(xs)
+        self._check(self.lib.cphf_mlp_features(self.h, p, nprop, None, 0, ctypes.byref(n)))
+        feat = np.zeros((n.value, 3), dtype=np.float32)
+        self._check(self.lib.cphf_mlp_features(self.h, p, nprop, ctypes.c_void_p(feat.ctypes.data), n.value,
+                                               ctypes.byref(n)))
+        return feat
+
+    def mlp_forward(self, feat, bf16=False):
+        feat = np.ascontiguousarray(feat, dtype=np.float32)
+        out = np.zeros((feat.shape[0], 2), dtype=np.float32)
+        self._check(self.lib.cphf_mlp_forward(self.h, ctypes.c_void_p(feat.ctypes.data), feat.shape[0],
+                                              ctypes.c_void_p(out.ctypes.data), 1 if bf16 else 0))
+        return out
+
+    def mlp_loss_grad(self, feat, target):
+        feat = np.ascontiguousarray(feat, dtype=np.float32)
+        target = np.ascontiguousarray(target, dtype=np.float32)
+        grad = np.zeros(MLP_NWEIGHTS, dtype=np.float32)
+        loss = ctypes.c_float()
+        self._check(self.lib.cphf_mlp_loss_grad(self.h, ctypes.c_void_p(feat.ctypes.data),
+                                                ctypes.c_void_p(target.ctypes.data), feat.shape[0],
+                                                ctypes.byref(loss), ctypes.c_void_p(grad.ctypes.data)))
+        return loss.value, grad
+
+    def mlp_train(self, feat, target, epochs=20, batch=4096, lr=1e-3, seed=0):
+        feat = np.ascontiguousarray(feat, dtype=np.float32)
+        target = np.ascontiguousarray(target, dtype=np.float32)
+        hist = np.zeros(max(epochs, 1), dtype=np.float32)
+        self._check(self.lib.cphf_mlp_train(self.h, ctypes.c_void_p(feat.ctypes.data),
+                                            ctypes.c_void_p(target.ctypes.data), feat.shape[0], epochs, batch,
+                                            lr, seed, ctypes.c_void_p(hist.ctypes.data)))
+        return hist[:epochs]

@@ -43,6 +43,8 @@ CONFIGS = {
     "rhf_nao24": dict(nao=24, naux=84, nocc=(5,), natm=4, decay=6.0),
     # nao=600, naux=2000, nocc=60, nrhs=180 (60 atoms), decay 20
     "rhf_nao600": dict(nao=600, naux=2000, nocc=(60,), natm=60, decay=20.0),
+    # half-size case for profiler captures: nao=300, naux=1000, nocc=30, nrhs=90
+    "rhf_nao300": dict(nao=300, naux=1000, nocc=(30,), natm=30, decay=20.0),
     # config above plus a ~660k-point LDA grid (60 atoms x 10 AOs)
     "rks_nao600": dict(nao=600, naux=2000, nocc=(60,), natm=60, decay=20.0, grid=True),
     # UHF/UKS: nao=800, naux=2700, nocc 80/78, 240 RHS (80 atoms)

@@ -7,6 +7,7 @@
 
 #include "ctx.cuh"
 #include "kernels.cuh"
+#include "mlp.cuh"
 
 using namespace cphf;
 
@@ -121,8 +122,9 @@ void check_finite(cphf_ctx* c, const double* dev, int64_t n, const char* what) {
 }  // namespace
 
 namespace cphf {
-// mixed-precision solve (defined in mixed.cu)
-bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, double* x, cphf_stats* st);
+// mixed-precision solve (defined in mixed.cu); m: optional left preconditioner of the inner solves
+bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, double* x, cphf_stats* st,
+                 const double* m);
 }
 
 extern "C" {
@@ -143,6 +145,9 @@ cphf_status cphf_config_default(cphf_config* cfg) {
   cfg->use_learned_guess = 0;
   cfg->verbose = 0;
   cfg->aux_chunk = 0;
+  cfg->tensor_cores = 1;
+  cfg->verify_residual = 1;
+  cfg->fp64_every_step = 0;
   return CPHF_OK;
 }
 
@@ -204,6 +209,49 @@ const char* cphf_last_error(const cphf_ctx* c) { return c ? c->last_error.c_str(
 void* cphf_ctx_stream(const cphf_ctx* c) { return c ? (void*)c->stream : nullptr; }
 int64_t cphf_ctx_device_bytes(const cphf_ctx* c) { return c ? c->device_bytes : 0; }
 int64_t cphf_ctx_kernel_launches(const cphf_ctx* c) { return c ? c->launches : 0; }
+
+int32_t cphf_ctx_tensor_cores_active(const cphf_ctx* c) {
+  return (c && c->lowp && c->lowp->use_tc && c->has_rijk) ? 1 : 0;
+}
+
+cphf_status cphf_ctx_profile(cphf_ctx* c, int32_t enable) {
+  return guarded(c, [&] {
+    CPHF_CUDA(cudaStreamSynchronize(c->stream));
+    for (auto& r : c->prof.recs) {
+      c->prof.pool.push_back(r.start);
+      c->prof.pool.push_back(r.stop);
+    }
+    c->prof.recs.clear();
+    c->prof.on = enable != 0;
+  });
+}
+
+int32_t cphf_ctx_profile_report(cphf_ctx* c, cphf_prof_entry* out, int32_t max) {
+  if (!c) return -1;
+  int32_t n = 0;
+  cphf_status st = guarded(c, [&] {
+    CPHF_CUDA(cudaStreamSynchronize(c->stream));
+    cphf_prof_entry acc[PROF_NCLASS];
+    std::memset(acc, 0, sizeof(acc));
+    for (const auto& r : c->prof.recs) {
+      float ms = 0.f;
+      CPHF_CUDA(cudaEventElapsedTime(&ms, r.start, r.stop));
+      cphf_prof_entry& e = acc[r.cls];
+      e.launches += 1;
+      e.ms += ms;
+      e.max_ms = std::max(e.max_ms, (double)ms);
+      e.flops += r.flops;
+      e.bytes += r.bytes;
+    }
+    for (int k = 0; k < PROF_NCLASS && n < max; ++k) {
+      if (acc[k].launches == 0) continue;
+      std::strncpy(acc[k].name, kProfNames[k], sizeof(acc[k].name) - 1);
+      if (out) out[n] = acc[k];
+      ++n;
+    }
+  });
+  return st == CPHF_OK ? n : -1;
+}
 
 cphf_status cphf_ctx_synchronize(cphf_ctx* c) {
   return guarded(c, [&] { CPHF_CUDA(cudaStreamSynchronize(c->stream)); });
@@ -380,16 +428,18 @@ cphf_status cphf_plugin_response_bra(cphf_ctx* c, int32_t which, const double* c
 }
 
 static cphf_status response_mo_common(cphf_ctx* c, const double* const* mo1, int64_t nprop,
-                                      double* const* resp, bool dimless) {
+                                      double* const* resp, bool dimless, bool lowp = false) {
   return guarded(c, [&] {
     require_prepared(c);
     CPHF_CHECK_ARG(mo1 && resp, "null arrays");
+    if (lowp) CPHF_CHECK_ARG(c->cfg.precision == CPHF_PRECISION_MIXED, "the context is not in mixed precision");
     const int64_t n = krylov_n(c);
     c->s_host_io.ensure((size_t)std::max<int64_t>(n * nprop, 1) * 8 * 2, c->counter());
     double* x = c->s_host_io.as<double>();
     double* y = x + n * nprop;
     pack_krylov(c, mo1, nprop, x);
-    if (nprop > 0) response_mo_fp64(c, x, nprop, y, dimless);
+    if (nprop > 0 && lowp) response_mo_lowp(c, x, nprop, y);
+    else if (nprop > 0) response_mo_fp64(c, x, nprop, y, dimless);
     unpack_krylov(c, y, nprop, resp);
     CPHF_CUDA(cudaStreamSynchronize(c->stream));
   });
@@ -401,6 +451,10 @@ cphf_status cphf_response_mo(cphf_ctx* c, const double* const* mo1, int64_t npro
 
 cphf_status cphf_response_dimless(cphf_ctx* c, const double* const* mo1, int64_t nprop, double* const* resp) {
   return response_mo_common(c, mo1, nprop, resp, true);
+}
+
+cphf_status cphf_response_dimless_lowp(cphf_ctx* c, const double* const* mo1, int64_t nprop, double* const* resp) {
+  return response_mo_common(c, mo1, nprop, resp, true, true);
 }
 
 cphf_status cphf_solve_dimless_cphf(cphf_ctx* c, const double* const* rhs, int64_t nprop,
@@ -420,16 +474,37 @@ cphf_status cphf_solve_dimless_cphf(cphf_ctx* c, const double* const* rhs, int64
     pack_krylov(c, rhs, nprop, b);
     check_finite(c, b, n * nprop, "rhs");
     if (x0) pack_krylov(c, x0, nprop, xg);
+    const double* x0p = x0 ? xg : nullptr;
+    // learned initial guess and left preconditioner (the unpreconditioned FP64 residual stays the judge)
+    DevBuf pre;
+    double* m = nullptr;
+    if (c->cfg.use_learned_guess) {
+      mlp_require(c);
+      if (c->spin[0].iaia.p == nullptr) mlp_prepare_iaia(c);
+      pre.ensure((size_t)n * 8 * (1 + nprop), c->counter());
+      m = pre.as<double>();
+      double* guess = m + n;
+      mlp_guess(c, b, nprop, guess, m);
+      if (!x0p) x0p = guess;
+    }
     if (c->cfg.precision == CPHF_PRECISION_MIXED) {
-      converged = solve_mixed(c, b, x0 ? xg : nullptr, nprop, x, &st);
+      converged = solve_mixed(c, b, x0p, nprop, x, &st, m);
     } else {
       KrylovParams p{c->cfg.cphf_tol, c->cfg.cphf_lindep, c->cfg.cphf_max_cycle, c->cfg.cphf_max_space,
                      c->cfg.verbose != 0};
       DeviceOp op = [&](const double* xin, int64_t nb, double* yout) {
         response_mo_fp64(c, xin, nb, yout, true);
+        if (m) launch_apply_precond(m, xin, yout, n, nb, c->stream);
         st.fp64_matvec_columns += nb;
       };
-      converged = krylov_device(c, op, b, x0 ? xg : nullptr, n, nprop, p, x, &st);
+      const double* bp = b;
+      DevBuf bm;
+      if (m) {
+        bm.ensure((size_t)n * nprop * 8, c->counter());
+        launch_scale_rows_by(m, b, bm.as<double>(), n, nprop, c->stream);
+        bp = bm.as<double>();
+      }
+      converged = krylov_device(c, op, bp, x0p, n, nprop, p, x, &st);
       st.residual_max = -1.0;  // not evaluated by the plain solver (the reference does not either)
     }
     unpack_krylov(c, x, nprop, mo1);

@@ -21,13 +21,15 @@ struct LowpState {
   int64_t ldk = 0;             // padded row length of the BF16 copies
   DevBuf phi32;
   DevBuf s_c1, s_resp, s_T, s_W, s_d, s_ket, s_rho, s_y, s_x, s_Thi, s_Tlo, s_acc;
+  DevBuf err;                  // device error flag of the tensor-core kernels (bounded waits)
+  double sA = 1.0;             // power-of-two scale of the FP16 cderi planes
   bool use_tc = true;
 };
 
-// Learned initial guess / preconditioner weights (mlp.cu).
+// Learned initial guess / preconditioner (mlp.cu): weights, Adam moments, scratch.
 struct MlpState {
-  std::vector<float> host;
-  DevBuf w;
+  DevBuf w, m, v, g, part, idx, feat, out;
+  int64_t step = 0;
 };
 
 struct SpinState {
@@ -39,6 +41,7 @@ struct SpinState {
   DevBuf aobra;   // [ngrids, nocc] FP64: phi Cocc (XC)
   // split-precision copies (mixed path)
   DevBuf C32, Z32, O32, aobra32;
+  DevBuf iaia;    // [nvir, nocc] FP32: RI diagonal (ia|ia), feature of the learned guess
 };
 
 struct XcBatch {
@@ -49,6 +52,38 @@ struct XcBatch {
 
 // Operator over Krylov columns: y[:, 0:nb] = A x[:, 0:nb] with device pointers, ld = n.
 using DeviceOp = std::function<void(const double* x, int64_t nb, double* y)>;
+
+// Per-kernel-class timing with CUDA events on the context stream (the reference keeps
+// wall-clock (label, seconds) pairs, src/hessian/rscf.rs:33, src/ri_jk/hess_r.rs:192-198).
+struct ProfRecord {
+  int cls;
+  double flops, bytes;
+  cudaEvent_t start, stop;
+};
+struct Profiler {
+  bool on = false;
+  std::vector<ProfRecord> recs;
+  std::vector<cudaEvent_t> pool;
+  cudaEvent_t get() {
+    if (!pool.empty()) {
+      cudaEvent_t e = pool.back();
+      pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+  }
+  ~Profiler() {
+    for (auto& r : recs) {
+      cudaEventDestroy(r.start);
+      cudaEventDestroy(r.stop);
+    }
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+enum ProfClass { PROF_GEMM_F64 = 0, PROF_GEMM_F32 = 1, PROF_TC_KTERM = 2, PROF_NCLASS = 3 };
+extern const char* const kProfNames[PROF_NCLASS];
 
 }  // namespace cphf
 
@@ -88,9 +123,32 @@ struct cphf_ctx {
 
   std::unique_ptr<cphf::LowpState> lowp;
   std::unique_ptr<cphf::MlpState> mlp;
+  cphf::Profiler prof;
 
   int64_t* counter() { return &device_bytes; }
 };
+
+namespace cphf {
+// Scope that brackets one launch (or a group) with events when profiling is on.
+struct ProfScope {
+  cphf_ctx* c;
+  ProfRecord r{};
+  ProfScope(cphf_ctx* ctx, int cls, double flops, double bytes) : c(ctx) {
+    if (!c->prof.on) return;
+    r.cls = cls;
+    r.flops = flops;
+    r.bytes = bytes;
+    r.start = c->prof.get();
+    r.stop = c->prof.get();
+    cudaEventRecord(r.start, c->stream);
+  }
+  ~ProfScope() {
+    if (!c->prof.on) return;
+    cudaEventRecord(r.stop, c->stream);
+    c->prof.recs.push_back(r);
+  }
+};
+}  // namespace cphf
 
 namespace cphf {
 

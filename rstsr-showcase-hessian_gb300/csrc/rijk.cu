@@ -22,9 +22,14 @@
 
 namespace cphf {
 
+const char* const kProfNames[PROF_NCLASS] = {"gemm_fp64_simt", "gemm_fp32_simt", "kterm_tcgen05_f16x3"};
+
+static double gemm_flops(const GemmDesc& d) { return 2.0 * d.M * d.N * d.K * d.batch1 * d.batch2; }
+
 void gemm64(cphf_ctx* c, const GemmDesc& d) {
   const size_t need = gemm_workspace_bytes(d, 8, c->num_sms);
   if (need) c->ws_gemm.ensure(need, c->counter());
+  ProfScope ps(c, PROF_GEMM_F64, gemm_flops(d), 8.0 * (d.M * d.K + d.K * d.N + d.M * d.N) * d.batch1 * d.batch2);
   CPHF_CUDA((gemm<double, double, double, double>(d, c->stream, c->ws_gemm.p, c->ws_gemm.bytes, c->num_sms)));
 }
 
@@ -34,6 +39,7 @@ template <typename TA, typename TB, typename TC>
 void gemm32x(cphf_ctx* c, const GemmDesc& d) {
   const size_t need = gemm_workspace_bytes(d, 4, c->num_sms);
   if (need) c->ws_gemm.ensure(need, c->counter());
+  ProfScope ps(c, PROF_GEMM_F32, gemm_flops(d), 4.0 * (d.M * d.K + d.K * d.N + d.M * d.N) * d.batch1 * d.batch2);
   CPHF_CUDA((gemm<float, TA, TB, TC>(d, c->stream, c->ws_gemm.p, c->ws_gemm.bytes, c->num_sms)));
 }
 template void gemm32x<float, float, float>(cphf_ctx*, const GemmDesc&);

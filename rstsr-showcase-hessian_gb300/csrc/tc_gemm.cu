@@ -1,13 +1,457 @@
-// Tensor-core split-BF16 K-term contraction (placeholder until the tcgen05 kernel lands).
+// Tensor-core split-FP16 contraction of the RI-K term on sm_103a (tcgen05 + TMEM + TMA).
+//
+//   out[mu, n] += alpha * sum_P sum_nu B_P[mu, nu] T_P[nu, n],   T_P[nu, (i,a)] = sum_j bra[nu,j,a] O_P[j,i]
+//
+// which is term 1 of the exchange response, -sum_P (B_P bra_a) O_P (src/ri_jk/hess_r.rs:168-170).
+//
+// Precision: each FP64/FP32 operand x is scaled by a power of two s (|x s| <= 2^14) and
+// split into two FP16 planes, x s = hi + lo (hi = fp16(x s), lo = fp16(x s - hi)), a
+// 22-bit representation.  Three MMAs per K step, hi*hi + hi*lo + lo*hi, accumulate in
+// FP32 in tensor memory; the dropped lo*lo term and the FP32 accumulation leave ~1e-6
+// relative error, removed by the FP64 defect correction of the mixed solve.
+//
+// Kernel structure (one CTA per SM, 4 warps):
+//   warp 0 lane 0  -- TMA producer: 3-D tiled loads (K = nu, row = mu or n, P) of the four
+//                     planes into a 2-stage ring of 128B-swizzled shared-memory tiles;
+//   warp 1 lane 0  -- MMA issuer: tcgen05.mma.cta_group::1.kind::f16 (M=128, N=256, K=16),
+//                     tcgen05.commit frees a stage when its MMAs retire;
+//   warp 2         -- TMEM allocation (256 FP32 columns) and release;
+//   warps 0-3      -- epilogue: tcgen05.ld of the 128 x 256 accumulator, scaled and
+//                     atomically added to out (split over P ranges across CTAs).
+// Every mbarrier wait is bounded; on expiry the kernel records an error flag and returns.
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "kernels.cuh"
 #include "tc_gemm.cuh"
 
 namespace cphf {
+namespace {
 
-bool tc_available(cphf_ctx*) { return false; }
-void tc_prepare_cderi(cphf_ctx*, DevBuf&, DevBuf&, int64_t& ldk) { ldk = 0; }
-void tc_k_term1(cphf_ctx*, const DevBuf&, const DevBuf&, int64_t, const float*, const float*, int64_t,
-                int64_t, double, float*, DevBuf&, DevBuf&) {
-  throw Error(CPHF_ERR_STATE, "tensor-core path unavailable");
+constexpr int BM = 128, BN = 256, BK = 64;
+constexpr int STAGES = 2;
+constexpr int A_TILE = BM * BK * 2;  // bytes, FP16
+constexpr int B_TILE = BN * BK * 2;
+constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;  // hi + lo planes of both operands
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*barriers*/ + 1024 /*alignment*/;
+constexpr int TMEM_COLS = 256;
+constexpr uint32_t WAIT_LIMIT = 1u << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// Bounded parity wait; returns false (and raises *err) when the limit is reached.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err) {
+  for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if ((i & 1023) == 1023 && *(volatile int*)err) return false;
+  }
+  atomicExch(err, 1);
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int c0, int c1,
+                                            int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128B swizzle, 8-row groups 1024 B apart.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;             // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;             // descriptor version for tcgen05
+  d |= (uint64_t)2 << 61;             // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor: kind::f16, A/B FP16, D FP32, K-major A and B, M = 128, N = 256.
+__host__ __device__ constexpr uint32_t instr_desc() {
+  return (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct TcArgs {
+  float* out;
+  int64_t ld_out;   // out[mu + ld_out * n]
+  int M, N;         // mu rows (nao), n columns
+  int nkb;          // K blocks of 64 per aux function
+  int np;           // aux functions in this chunk
+  int p_per_cta;    // aux functions per CTA (P split)
+  int pA0;          // global aux index of the chunk's first function (A coordinate)
+  int m_tiles;
+  const float* scale;  // device: alpha / (sA * sT)
+  int* err;
+};
+
+__global__ void __launch_bounds__(128, 1)
+    tc_term1_kernel(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
+                    const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, TcArgs args) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 8);
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES), accum = smem_u32(bars + 2 * STAGES);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m_tile = blockIdx.x % args.m_tiles, n_tile = blockIdx.x / args.m_tiles;
+  const int m0 = m_tile * BM, n0 = n_tile * BN;
+  const int pbeg = blockIdx.y * args.p_per_cta;
+  const int pend = min(args.np, pbeg + args.p_per_cta);
+  const int total = (pend - pbeg) * args.nkb;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    mbar_init(accum, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 2) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (total > 0) {
+    if (warp == 0 && lane == 0) {
+      // producer
+      int issued = 0;
+      for (int it = 0; it < total; ++it) {
+        const int s = it % STAGES;
+        const uint32_t ph = (it / STAGES) & 1;
+        if (!mbar_wait(empty0 + 8 * s, ph ^ 1, args.err)) break;
+        issued = it + 1;
+        const uint32_t full = full0 + 8 * s;
+        mbar_expect_tx(full, STAGE_BYTES);
+        const int P = pbeg + it / args.nkb;
+        const int k0 = (it % args.nkb) * BK;
+        uint8_t* st = smem + s * STAGE_BYTES;
+        tma_load_3d(smem_u32(st), &mAh, full, k0, m0, args.pA0 + P);
+        tma_load_3d(smem_u32(st + A_TILE), &mAl, full, k0, m0, args.pA0 + P);
+        tma_load_3d(smem_u32(st + 2 * A_TILE), &mBh, full, k0, n0, P);
+        tma_load_3d(smem_u32(st + 2 * A_TILE + B_TILE), &mBl, full, k0, n0, P);
+      }
+      // drain: the copies of the last round of every stage have landed before the CTA may exit
+      for (int it = max(0, issued - STAGES); it < issued; ++it) {
+        int dummy = 0;
+        mbar_wait(full0 + 8 * (it % STAGES), (it / STAGES) & 1, &dummy);
+      }
+    } else if (warp == 1 && lane == 0) {
+      // MMA issuer
+      constexpr uint32_t idesc = instr_desc();
+      bool ok = true;
+      for (int it = 0; it < total; ++it) {
+        const int s = it % STAGES;
+        const uint32_t ph = (it / STAGES) & 1;
+        if (!mbar_wait(full0 + 8 * s, ph, args.err)) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+        const uint64_t ah = smem_desc(st), al = smem_desc(st + A_TILE);
+        const uint64_t bh = smem_desc(st + 2 * A_TILE), bl = smem_desc(st + 2 * A_TILE + B_TILE);
+#pragma unroll
+        for (int k = 0; k < BK / 16; ++k) {
+          const uint64_t dk = (uint64_t)((k * 32) >> 4);  // 16 FP16 = 32 B along K inside the swizzle atom
+          mma_f16(tmem, ah + dk, bh + dk, idesc, (it > 0 || k > 0) ? 1u : 0u);
+          mma_f16(tmem, ah + dk, bl + dk, idesc, 1u);
+          mma_f16(tmem, al + dk, bh + dk, idesc, 1u);
+        }
+        mma_commit(empty0 + 8 * s);
+      }
+      (void)ok;
+      mma_commit(accum);  // also covers an early exit: arrives when the issued MMAs retire
+    }
+    __syncwarp();
+    // epilogue: all four warps, warp w owns TMEM lanes [32 w, 32 w + 32)
+    const bool have = mbar_wait(accum, 0, args.err);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (have && *(volatile int*)args.err == 0) {
+      const float scale = *args.scale;
+      const int row = m0 + warp * 32 + lane;
+      for (int c = 0; c < BN / 32; ++c) {
+        float v[32];
+        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), v);
+        if (row < args.M) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int n = n0 + c * 32 + j;
+            if (n < args.N) atomicAdd(args.out + row + args.ld_out * (int64_t)n, scale * v[j]);
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (warp == 2) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+// ---- FP16 plane splitting --------------------------------------------------------------
+__device__ __forceinline__ void split_f16(double x, double s, __half* hi, __half* lo) {
+  const double xs = x * s;
+  const __half h = __double2half(xs);
+  *hi = h;
+  *lo = __double2half(xs - (double)__half2float(h));
+}
+
+// dense symmetric cderi (FP64 [P][mu][nu]) -> planes [P][mu][ldk] (nu contiguous)
+__global__ void split_cderi_kernel(const double* __restrict__ Bd, int64_t nao, int64_t naux, int64_t ldk, double s,
+                                   __half* __restrict__ hi, __half* __restrict__ lo) {
+  const int64_t total = naux * nao * ldk;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t nu = t % ldk;
+    const int64_t r = t / ldk;  // P * nao + mu
+    if (nu < nao) {
+      const int64_t P = r / nao, mu = r % nao;
+      split_f16(Bd[mu + nao * nu + nao * nao * P], s, hi + t, lo + t);
+    } else {
+      hi[t] = __float2half(0.f);
+      lo[t] = __float2half(0.f);
+    }
+  }
+}
+
+// |x| maxima: one atomicMax on the float bit pattern per block
+__global__ void absmax_f32_kernel(const float* __restrict__ x, int64_t n, int64_t row, int64_t valid,
+                                  unsigned* out) {
+  float m = 0.f;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    if (t % row < valid) m = fmaxf(m, fabsf(x[t]));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+__global__ void absmax_f64_kernel(const double* __restrict__ x, int64_t n, unsigned* out) {
+  float m = 0.f;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, (float)fabs(x[t]));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+// power-of-two scale bringing max |x| to at most 2^14; scale[0] = s, scale[1] = alpha / (sA * s)
+__device__ __forceinline__ float pow2_scale(float mx) {
+  if (!(mx > 0.f) || !isfinite(mx)) return 1.f;
+  int e;
+  frexpf(mx, &e);  // mx = f * 2^e, f in [0.5, 1)
+  return ldexpf(1.f, 14 - e);
+}
+
+__global__ void t_scale_kernel(const unsigned* mx, float sA, float alpha, float* scale) {
+  const float s = pow2_scale(__uint_as_float(*mx));
+  scale[0] = s;
+  scale[1] = alpha / (sA * s);
+}
+
+// T32 chunk [np][N][ldk] (FP32) -> planes, nu >= nao skipped (never read: outside the TMA extent)
+__global__ void split_t_kernel(const float* __restrict__ t32, int64_t n, const float* __restrict__ scale,
+                               __half* __restrict__ hi, __half* __restrict__ lo) {
+  const float s = scale[0];
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const float xs = t32[t] * s;
+    const __half h = __float2half_rn(xs);
+    hi[t] = h;
+    lo[t] = __float2half_rn(xs - __half2float(h));
+  }
+}
+
+// ---- host side ---------------------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+// 3-D FP16 tensor map: dims {K (= nao), rows, planes}, row stride ldk elements, 128B swizzle.
+CUtensorMap make_map(const void* base, int64_t K, int64_t rows, int64_t depth, int64_t ldk, int box_rows) {
+  CUtensorMap m;
+  std::memset(&m, 0, sizeof(m));
+  auto fn = encode_fn();
+  if (!fn) throw Error(CPHF_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)depth};
+  cuuint64_t strides[2] = {(cuuint64_t)(ldk * 2), (cuuint64_t)(ldk * 2 * rows)};
+  cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw Error(CPHF_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return m;
+}
+
+unsigned grid_for(int64_t total) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(div_up(total, 256), 1 << 20)); }
+
+}  // namespace
+
+bool tc_available(cphf_ctx* c) {
+  int major = 0, minor = 0;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, c->device);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, c->device);
+  if (major != 10 || encode_fn() == nullptr) return false;
+  static bool attr_set = false;
+  if (!attr_set) {
+    if (cudaFuncSetAttribute(tc_term1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    attr_set = true;
+  }
+  return true;
+}
+
+void tc_prepare_cderi(cphf_ctx* c, DevBuf& hi, DevBuf& lo, int64_t& ldk) {
+  const int64_t nao = c->nao, naux = c->naux;
+  ldk = (nao + 7) / 8 * 8;
+  // power-of-two scale from max |B|
+  DevBuf mx;
+  mx.ensure(sizeof(unsigned), nullptr);
+  CPHF_CUDA(cudaMemsetAsync(mx.p, 0, sizeof(unsigned), c->stream));
+  absmax_f64_kernel<<<grid_for(nao * nao * naux), 256, 0, c->stream>>>(c->Bd.as<double>(), nao * nao * naux, mx.as<unsigned>());
+  unsigned bits = 0;
+  CPHF_CUDA(cudaMemcpyAsync(&bits, mx.p, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  CPHF_CUDA(cudaStreamSynchronize(c->stream));
+  float m;
+  std::memcpy(&m, &bits, 4);
+  int e = 0;
+  std::frexp((double)m, &e);
+  const double sA = (m > 0.f) ? std::ldexp(1.0, 14 - e) : 1.0;
+  c->lowp->sA = sA;
+  const size_t bytes = (size_t)naux * nao * ldk * 2;
+  hi.ensure(bytes, c->counter());
+  lo.ensure(bytes, c->counter());
+  split_cderi_kernel<<<grid_for(naux * nao * ldk), 256, 0, c->stream>>>(c->Bd.as<double>(), nao, naux, ldk, sA,
+                                                                       hi.as<__half>(), lo.as<__half>());
+  count_launch(2);
+  CPHF_CUDA(cudaGetLastError());
+}
+
+void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, const float* O32, const float* bra,
+                int64_t no, int64_t nb, double alpha, float* out, DevBuf& Thi, DevBuf& Tlo) {
+  LowpState& L = *c->lowp;
+  const int64_t nao = c->nao, naux = c->naux;
+  const int64_t N = no * nb;
+  // aux functions per chunk: T planes bounded by ~1 GiB, batched T generation within grid limits
+  int64_t np = std::max<int64_t>(1, (int64_t(1) << 30) / std::max<int64_t>(N * ldk * 4, 1));
+  np = std::min<int64_t>(np, std::max<int64_t>(1, 65535 / std::max<int64_t>(nb, 1)));
+  np = std::min<int64_t>(np, naux);
+  const size_t plane = (size_t)np * N * ldk * 2;
+  Thi.ensure(plane, c->counter());
+  Tlo.ensure(plane, c->counter());
+  L.s_acc.ensure((size_t)np * N * ldk * 4 + 64, c->counter());  // T32 staging + scale scratch
+  float* T32 = L.s_acc.as<float>();
+  unsigned* mx = reinterpret_cast<unsigned*>(T32 + (size_t)np * N * ldk);
+  float* scale = reinterpret_cast<float*>(mx + 4);
+  L.err.ensure(sizeof(int), c->counter());
+  const int m_tiles = (int)div_up(nao, BM), n_tiles = (int)div_up(N, BN);
+  const int nkb = (int)div_up(nao, BK);
+  const int ppc = 16;
+  for (int64_t P0 = 0; P0 < naux; P0 += np) {
+    const int64_t npc = std::min<int64_t>(np, naux - P0);
+    // T32[Pl][(i,a)][nu] = sum_j bra[nu, j, a] O_P[j, i]
+    GemmDesc t;
+    t.M = nao; t.N = no; t.K = no; t.batch1 = npc; t.batch2 = nb;
+    t.A = bra; t.a_m = 1; t.a_k = nao; t.a_b1 = 0; t.a_b2 = nao * no;
+    t.B = O32 + P0 * no * no; t.b_k = 1; t.b_n = no; t.b_b1 = no * no; t.b_b2 = 0;
+    t.C = T32; t.c_m = 1; t.c_n = ldk; t.c_b1 = N * ldk; t.c_b2 = no * ldk;
+    gemm32(c, t);
+    const int64_t tn = npc * N * ldk;
+    CPHF_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned), c->stream));
+    absmax_f32_kernel<<<grid_for(tn), 256, 0, c->stream>>>(T32, tn, ldk, nao, mx);
+    t_scale_kernel<<<1, 1, 0, c->stream>>>(mx, (float)L.sA, (float)alpha, scale);
+    split_t_kernel<<<grid_for(tn), 256, 0, c->stream>>>(T32, tn, scale, Thi.as<__half>(), Tlo.as<__half>());
+    count_launch(3);
+    const CUtensorMap mAh = make_map(Bhi.p, nao, nao, naux, ldk, BM);
+    const CUtensorMap mAl = make_map(Blo.p, nao, nao, naux, ldk, BM);
+    const CUtensorMap mBh = make_map(Thi.p, nao, N, npc, ldk, BN);
+    const CUtensorMap mBl = make_map(Tlo.p, nao, N, npc, ldk, BN);
+    TcArgs a;
+    a.out = out;
+    a.ld_out = nao;
+    a.M = (int)nao;
+    a.N = (int)N;
+    a.nkb = nkb;
+    a.np = (int)npc;
+    a.p_per_cta = ppc;
+    a.pA0 = (int)P0;
+    a.m_tiles = m_tiles;
+    a.scale = scale + 1;
+    a.err = L.err.as<int>();
+    dim3 grid((unsigned)(m_tiles * n_tiles), (unsigned)div_up(npc, ppc));
+    // algorithmic FLOPs of the contraction (the tensor pipe executes three split products);
+    // bytes: the FP16 planes of both operands read once
+    ProfScope ps(c, PROF_TC_KTERM, 2.0 * nao * N * nao * npc, 4.0 * nao * npc * (nao + N));
+    tc_term1_kernel<<<grid, 128, SMEM_BYTES, c->stream>>>(mAh, mAl, mBh, mBl, a);
+    count_launch();
+    CPHF_CUDA(cudaGetLastError());
+  }
 }
 
 }  // namespace cphf
