@@ -66,6 +66,10 @@ typedef struct cphf_config {
   int32_t tensor_cores;      /* mixed: 1 = tcgen05 split-FP16 K term (default), 0 = FP32 CUDA cores */
   int32_t verify_residual;   /* mixed: recompute the final residual with the FP64 operator (default 1) */
   int32_t fp64_every_step;   /* mixed: FP64 residual after every correction, not only the first (default 0) */
+  int64_t xc_chunk_points;   /* grid points per XC chunk (default 0 = 8 GiB of intermediates) */
+  int32_t residual_dfloat;   /* mixed: the correction residuals in double-float arithmetic on the FP32
+                                pipes (~1e-14 relative, default 1); 0 = native FP64.  The final
+                                verification (verify_residual) is always native FP64. */
 } cphf_config;
 
 /* Solver statistics (the reference reports them by println!, krylov_block.rs:148-151, 175). */
@@ -200,6 +204,7 @@ cphf_status cphf_dense_op_destroy(cphf_dense_op* op);
 
 /* Copy `bytes` between any host / device pointers on the context's stream and wait. */
 cphf_status cphf_copy(cphf_ctx* ctx, void* dst, const void* src, int64_t bytes);
+
 
 /* ---- learned initial guess / preconditioner (no counterpart in the reference) ------------ */
 /* Per-(i,a)-pair MLP 3 -> 64 -> 64 -> 2 (GELU), FP32 weights packed as

@@ -70,6 +70,8 @@ class Config(ctypes.Structure):
         ("tensor_cores", ctypes.c_int32),
         ("verify_residual", ctypes.c_int32),
         ("fp64_every_step", ctypes.c_int32),
+        ("xc_chunk_points", ctypes.c_int64),
+        ("residual_dfloat", ctypes.c_int32),
     ]
 
 

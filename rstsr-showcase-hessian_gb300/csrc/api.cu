@@ -148,6 +148,8 @@ cphf_status cphf_config_default(cphf_config* cfg) {
   cfg->tensor_cores = 1;
   cfg->verify_residual = 1;
   cfg->fp64_every_step = 0;
+  cfg->xc_chunk_points = 0;
+  cfg->residual_dfloat = 1;
   return CPHF_OK;
 }
 
@@ -350,6 +352,7 @@ cphf_status cphf_xc_set_grid(cphf_ctx* c, const double* ao, const double* weight
     copy_in(c, c->fxc.p, fxc, (size_t)nf * 8);
     CPHF_CUDA(cudaStreamSynchronize(c->stream));
     c->xc_batches = batches;
+    for (auto& pl : c->xc_plan) pl.key[0] = -1;  // chunk plans depend on the batches
     c->ngrids = ngrids;
     c->xc_nspin = nspin;
     c->has_xc = true;

@@ -50,6 +50,20 @@ struct XcBatch {
   int64_t phi_off = 0;        // element offset of the batch block in phi
 };
 
+// Chunking of the grid batches for one output width (xc_grouped.cu), cached per key.
+struct XcChunk {
+  int64_t b0, b1;         // batches [b0, b1)
+  int64_t g0, npts;       // grid points [g0, g0 + npts)
+  int64_t group_off;      // offset of the chunk's group records (per spin) in the device table
+  int64_t tiles[2];       // work items of the first GEMM, per spin
+};
+struct XcPlan {
+  int64_t key[4] = {-1, -1, -1, -1};  // element size, nb, nocc_a, nocc_b
+  std::vector<XcChunk> chunks;
+  DevBuf groups;                       // XcGroupDev records
+  int64_t max_pts = 0;
+};
+
 // Operator over Krylov columns: y[:, 0:nb] = A x[:, 0:nb] with device pointers, ld = n.
 using DeviceOp = std::function<void(const double* x, int64_t nb, double* y)>;
 
@@ -82,7 +96,7 @@ struct Profiler {
     for (auto e : pool) cudaEventDestroy(e);
   }
 };
-enum ProfClass { PROF_GEMM_F64 = 0, PROF_GEMM_F32 = 1, PROF_TC_KTERM = 2, PROF_NCLASS = 3 };
+enum ProfClass { PROF_GEMM_F64 = 0, PROF_GEMM_F32 = 1, PROF_TC_KTERM = 2, PROF_GEMM_F64E = 3, PROF_NCLASS = 4 };
 extern const char* const kProfNames[PROF_NCLASS];
 
 }  // namespace cphf
@@ -110,6 +124,7 @@ struct cphf_ctx {
   std::vector<cphf::XcBatch> xc_batches;
   cphf::DevBuf phi, weights, fxc;  // phi: batch blocks [npts_b, nwin_b] (grid fastest)
   cphf::DevBuf phi32;
+  cphf::XcPlan xc_plan[2];         // FP64 / FP32 chunk plans
 
   // prepared orbitals
   bool prepared = false;
@@ -124,6 +139,7 @@ struct cphf_ctx {
   std::unique_ptr<cphf::LowpState> lowp;
   std::unique_ptr<cphf::MlpState> mlp;
   cphf::Profiler prof;
+  bool f64_emulate = false;  // route the FP64 GEMMs through the double-float kernel
 
   int64_t* counter() { return &device_bytes; }
 };

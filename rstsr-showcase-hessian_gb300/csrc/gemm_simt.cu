@@ -5,24 +5,97 @@
 #include <algorithm>
 
 namespace cphf {
+
+// Double-float number for FP64-accurate products on the FP32 pipes.  A value is hi + lo
+// (two floats).  The product of two such numbers keeps ah*bh exactly (FMA error term) plus
+// the cross terms ah*bl + al*bh; accumulation is compensated summation (error-free
+// two-sum of the high parts, Ogita-Rump-Oishi Dot2), so a K-term dot product carries
+// about 2^-48 relative error per term instead of FP32's 2^-24.  Doubles are split with
+// integer operations (no FP64 instruction per element).
+struct dfloat {
+  float hi, lo;
+  dfloat() = default;
+  __device__ __forceinline__ dfloat(float h, float l) : hi(h), lo(l) {}
+  __device__ __forceinline__ explicit dfloat(int v) : hi((float)v), lo(0.f) {}
+  __device__ __forceinline__ explicit dfloat(double x) {
+    const unsigned int h32 = (unsigned int)__double2hiint(x), l32 = (unsigned int)__double2loint(x);
+    const unsigned int sign = h32 & 0x80000000u;
+    const int e = (int)((h32 >> 20) & 0x7FFu);
+    const int E = e - 1023 + 127;  // float biased exponent of hi
+    if (e == 0 || E <= 0) {        // zero, or below the normal float range (|x| < 2^-126): negligible here
+      hi = 0.f;
+      lo = 0.f;
+      return;
+    }
+    if (E >= 255) {  // beyond the float range: let it propagate as infinity
+      hi = __int_as_float((int)(sign | 0x7F800000u));
+      lo = 0.f;
+      return;
+    }
+    const unsigned int mant23 = ((h32 & 0xFFFFFu) << 3) | (l32 >> 29);
+    hi = __int_as_float((int)(sign | ((unsigned)E << 23) | mant23));
+    // remaining 29 mantissa bits: value r * 2^(e - 1075)
+    const unsigned int r = l32 & 0x1FFFFFFFu;
+    const int El = e - 1075 + 127;
+    if (r == 0u || El <= 0) {
+      lo = 0.f;
+    } else {
+      const float rf = __uint2float_rn(r) * __int_as_float(El << 23);
+      lo = sign ? -rf : rf;
+    }
+  }
+  __device__ __forceinline__ explicit operator double() const { return (double)hi + (double)lo; }
+  __device__ __forceinline__ bool operator!=(const dfloat& o) const { return hi != o.hi || lo != o.lo; }
+  __device__ __forceinline__ dfloat& operator+=(const dfloat& b) {
+    const float s = hi + b.hi;
+    const float z = s - hi;
+    const float t = (hi - (s - z)) + (b.hi - z);
+    hi = s;
+    lo = lo + (t + b.lo);
+    return *this;
+  }
+};
+
+__device__ __forceinline__ dfloat madd(const dfloat& a, const dfloat& b, const dfloat& c) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  const float s = c.hi + p;
+  const float z = s - c.hi;
+  const float t = (c.hi - (s - z)) + (p - z);
+  return dfloat(s, c.lo + (t + e));
+}
+
+__device__ __forceinline__ dfloat operator*(const dfloat& a, const dfloat& b) { return madd(a, b, dfloat(0)); }
+__device__ __forceinline__ double madd(double a, double b, double c) { return ::fma(a, b, c); }
+__device__ __forceinline__ float madd(float a, float b, float c) { return fmaf(a, b, c); }
+
 namespace {
 
-template <typename T>
-struct TileCfg;
 // FP64: 64x64 tile, 4x4 per thread, 256 threads.  FP64-pipe bound on GB300.
-template <>
-struct TileCfg<double> {
+struct CfgF64 {
   static constexpr int BM = 64, BN = 64, BK = 16, TM = 4, TN = 4;
 };
 // FP32: 128x128 tile, 8x8 per thread, 256 threads.
-template <>
-struct TileCfg<float> {
+struct CfgF32 {
   static constexpr int BM = 128, BN = 128, BK = 16, TM = 8, TN = 8;
 };
+// FP32 for narrow outputs (N <= 64, e.g. the occupied index of the K-term intermediates):
+// 256x64 tile, 8x8 per thread, 256 threads.
+struct CfgF32Tall {
+  static constexpr int BM = 256, BN = 64, BK = 16, TM = 8, TN = 8;
+};
 
-template <typename T, typename TA, typename TB, typename TC>
+// offset of row m (or column n) with optional two-level index m = m0 + div * m1
+__device__ __forceinline__ int64_t off2(int64_t m, int64_t div, int64_t s1, int64_t s2) {
+  if (div <= 0) return m * s1;
+  const int64_t q = m / div;
+  return (m - q * div) * s1 + q * s2;
+}
+
+template <typename T, typename Cfg, typename TA, typename TB, typename TC>
 __global__ void __launch_bounds__(256) gemm_kernel(GemmDesc d, int ksplit, int64_t kchunk, T* ws) {
-  using Cfg = TileCfg<T>;
   constexpr int BM = Cfg::BM, BN = Cfg::BN, BK = Cfg::BK, TM = Cfg::TM, TN = Cfg::TN;
   constexpr int NTX = BN / TN, NTY = BM / TM, NT = NTX * NTY;
   constexpr int LA = BM * BK / NT, LB = BK * BN / NT;
@@ -44,43 +117,50 @@ __global__ void __launch_bounds__(256) gemm_kernel(GemmDesc d, int ksplit, int64
 
   const int64_t kbeg = (int64_t)split * kchunk;
   const int64_t kend = min(d.K, kbeg + kchunk);
+  // load mapping: consecutive threads along the unit-stride index (offsets are precomputed, so
+  // a two-level index still coalesces inside each contiguous block)
   const bool a_mfast = (d.a_m == 1);
   const bool b_nfast = (d.b_n == 1);
+
+  // per-thread fixed row / column of each load, and its offset
+  int a_mm[LA], a_kk[LA], b_nn[LB], b_kk[LB];
+  int64_t a_off[LA], b_off[LB];
+  bool a_ok[LA], b_ok[LB];
+#pragma unroll
+  for (int i = 0; i < LA; ++i) {
+    const int e = tid + i * NT;
+    if (a_mfast) { a_mm[i] = e % BM; a_kk[i] = e / BM; } else { a_kk[i] = e % BK; a_mm[i] = e / BK; }
+    const int64_t gm = m0 + a_mm[i];
+    a_ok[i] = gm < d.M;
+    a_off[i] = a_ok[i] ? off2(gm, d.m_div, d.a_m, d.a_m2) : 0;
+  }
+#pragma unroll
+  for (int i = 0; i < LB; ++i) {
+    const int e = tid + i * NT;
+    if (b_nfast) { b_nn[i] = e % BN; b_kk[i] = e / BN; } else { b_kk[i] = e % BK; b_nn[i] = e / BK; }
+    const int64_t gn = n0 + b_nn[i];
+    b_ok[i] = gn < d.N;
+    b_off[i] = b_ok[i] ? off2(gn, d.n_div, d.b_n, d.b_n2) : 0;
+  }
 
   T ra[LA], rb[LB];
   auto load_tiles = [&](int64_t k0) {
 #pragma unroll
     for (int i = 0; i < LA; ++i) {
-      const int e = tid + i * NT;
-      int mm, kk;
-      if (a_mfast) { mm = e % BM; kk = e / BM; } else { kk = e % BK; mm = e / BK; }
-      const int64_t gm = m0 + mm, gk = k0 + kk;
-      ra[i] = (gm < d.M && gk < kend) ? (T)A[gm * d.a_m + gk * d.a_k] : (T)0;
+      const int64_t gk = k0 + a_kk[i];
+      ra[i] = (a_ok[i] && gk < kend) ? (T)A[a_off[i] + gk * d.a_k] : (T)0;
     }
 #pragma unroll
     for (int i = 0; i < LB; ++i) {
-      const int e = tid + i * NT;
-      int nn, kk;
-      if (b_nfast) { nn = e % BN; kk = e / BN; } else { kk = e % BK; nn = e / BK; }
-      const int64_t gn = n0 + nn, gk = k0 + kk;
-      rb[i] = (gn < d.N && gk < kend) ? (T)B[gk * d.b_k + gn * d.b_n] : (T)0;
+      const int64_t gk = k0 + b_kk[i];
+      rb[i] = (b_ok[i] && gk < kend) ? (T)B[b_off[i] + gk * d.b_k] : (T)0;
     }
   };
   auto store_tiles = [&](int buf) {
 #pragma unroll
-    for (int i = 0; i < LA; ++i) {
-      const int e = tid + i * NT;
-      int mm, kk;
-      if (a_mfast) { mm = e % BM; kk = e / BM; } else { kk = e % BK; mm = e / BK; }
-      As[buf][kk][mm] = ra[i];
-    }
+    for (int i = 0; i < LA; ++i) As[buf][a_kk[i]][a_mm[i]] = ra[i];
 #pragma unroll
-    for (int i = 0; i < LB; ++i) {
-      const int e = tid + i * NT;
-      int nn, kk;
-      if (b_nfast) { nn = e % BN; kk = e / BN; } else { kk = e % BK; nn = e / BK; }
-      Bs[buf][kk][nn] = rb[i];
-    }
+    for (int i = 0; i < LB; ++i) Bs[buf][b_kk[i]][b_nn[i]] = rb[i];
   };
 
   T acc[TM][TN];
@@ -107,7 +187,7 @@ __global__ void __launch_bounds__(256) gemm_kernel(GemmDesc d, int ksplit, int64
 #pragma unroll
         for (int i = 0; i < TM; ++i)
 #pragma unroll
-          for (int j = 0; j < TN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+          for (int j = 0; j < TN; ++j) acc[i][j] = madd(a[i], b[j], acc[i][j]);
       }
       if (has_next) {
         store_tiles(buf ^ 1);
@@ -123,13 +203,14 @@ __global__ void __launch_bounds__(256) gemm_kernel(GemmDesc d, int ksplit, int64
     for (int i = 0; i < TM; ++i) {
       const int64_t gm = m0 + ty + i * NTY;
       if (gm >= d.M) continue;
+      const int64_t cm = off2(gm, d.m_div, d.c_m, d.c_m2);
 #pragma unroll
       for (int j = 0; j < TN; ++j) {
         const int64_t gn = n0 + tx + j * NTX;
         if (gn >= d.N) continue;
-        TC* p = C + gm * d.c_m + gn * d.c_n;
+        TC* p = C + cm + off2(gn, d.n_div, d.c_n, d.c_n2);
         T v = alpha * acc[i][j];
-        if (beta != (T)0) v = fma(beta, (T)(*p), v);
+        if (beta != (T)0) v = madd(beta, (T)(*p), v);
         *p = (TC)v;
       }
     }
@@ -163,16 +244,16 @@ __global__ void splitk_reduce_kernel(GemmDesc d, int ksplit, const T* __restrict
     const int64_t b1 = bidx % d.batch1, b2 = bidx / d.batch1;
     T s = (T)0;
     for (int k = 0; k < ksplit; ++k) s += ws[(int64_t)k * total + e];
-    TC* p = static_cast<TC*>(d.C) + b1 * d.c_b1 + b2 * d.c_b2 + m * d.c_m + n * d.c_n;
+    TC* p = static_cast<TC*>(d.C) + b1 * d.c_b1 + b2 * d.c_b2 + off2(m, d.m_div, d.c_m, d.c_m2) +
+            off2(n, d.n_div, d.c_n, d.c_n2);
     T v = alpha * s;
-    if (beta != (T)0) v = fma(beta, (T)(*p), v);
+    if (beta != (T)0) v = madd(beta, (T)(*p), v);
     *p = (TC)v;
   }
 }
 
-template <typename T>
+template <typename Cfg>
 int choose_split(const GemmDesc& d, int num_sms) {
-  using Cfg = TileCfg<T>;
   const int64_t tiles = ((d.M + Cfg::BM - 1) / Cfg::BM) * ((d.N + Cfg::BN - 1) / Cfg::BN) *
                         d.batch1 * d.batch2;
   if (tiles >= 2 * (int64_t)num_sms) return 1;
@@ -183,29 +264,10 @@ int choose_split(const GemmDesc& d, int num_sms) {
   return (int)std::max<int64_t>(want, 1);
 }
 
-}  // namespace
-
-size_t gemm_workspace_bytes(const GemmDesc& d, size_t elem_bytes, int num_sms) {
-  const int s = elem_bytes == 8 ? choose_split<double>(d, num_sms) : choose_split<float>(d, num_sms);
-  if (s <= 1) return 0;
-  return (size_t)s * d.batch1 * d.batch2 * d.M * d.N * elem_bytes;
-}
-
-template <typename T, typename TA, typename TB, typename TC>
-cudaError_t gemm(const GemmDesc& d, cudaStream_t stream, void* workspace, size_t ws_bytes,
-                 int num_sms) {
-  using Cfg = TileCfg<T>;
-  if (d.M <= 0 || d.N <= 0) return cudaSuccess;
+template <typename T, typename Cfg, typename TA, typename TB, typename TC>
+cudaError_t run(const GemmDesc& d, cudaStream_t stream, void* workspace, size_t ws_bytes, int num_sms) {
   const int64_t nb = d.batch1 * d.batch2;
-  if (d.K <= 0) {
-    // C = beta * C (alpha term is empty)
-    GemmDesc z = d;
-    z.K = 0;
-    splitk_reduce_kernel<T, TC><<<std::max<int64_t>(1, std::min<int64_t>(4096, (nb * d.M * d.N + 255) / 256)), 256, 0, stream>>>(z, 0, (const T*)nullptr);
-    count_launch();
-    return cudaGetLastError();
-  }
-  int ksplit = choose_split<T>(d, num_sms);
+  int ksplit = choose_split<Cfg>(d, num_sms);
   if (ksplit > 1) {
     const size_t need = (size_t)ksplit * nb * d.M * d.N * sizeof(T);
     if (workspace == nullptr || need > ws_bytes) ksplit = 1;
@@ -222,7 +284,6 @@ cudaError_t gemm(const GemmDesc& d, cudaStream_t stream, void* workspace, size_t
     const int64_t bn = std::min<int64_t>(zmax, nb - b0);
     GemmDesc s = d;
     if (b0 != 0 || bn != nb) {
-      // flatten to batch1-only indexing for this slice when batch2 == 1
       if (d.batch2 != 1) return cudaErrorInvalidConfiguration;
       s.A = static_cast<const char*>(d.A) + b0 * d.a_b1 * (int64_t)sizeof(TA);
       s.B = static_cast<const char*>(d.B) + b0 * d.b_b1 * (int64_t)sizeof(TB);
@@ -230,7 +291,7 @@ cudaError_t gemm(const GemmDesc& d, cudaStream_t stream, void* workspace, size_t
       s.batch1 = bn;
     }
     dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)(bn * ksplit));
-    gemm_kernel<T, TA, TB, TC><<<grid, 256, 0, stream>>>(s, ksplit, kchunk, static_cast<T*>(workspace));
+    gemm_kernel<T, Cfg, TA, TB, TC><<<grid, 256, 0, stream>>>(s, ksplit, kchunk, static_cast<T*>(workspace));
     count_launch();
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) return err;
@@ -246,6 +307,39 @@ cudaError_t gemm(const GemmDesc& d, cudaStream_t stream, void* workspace, size_t
   return cudaSuccess;
 }
 
+// narrow-output FP32 shapes take the 256 x 64 tile
+bool use_tall(const GemmDesc& d) { return d.N <= 64 && d.M >= 512; }
+
+}  // namespace
+
+size_t gemm_workspace_bytes(const GemmDesc& d, size_t elem_bytes, int num_sms) {
+  int s;
+  if (elem_bytes == 8) s = choose_split<CfgF64>(d, num_sms);
+  else s = use_tall(d) ? choose_split<CfgF32Tall>(d, num_sms) : choose_split<CfgF32>(d, num_sms);
+  if (s <= 1) return 0;
+  return (size_t)s * d.batch1 * d.batch2 * d.M * d.N * elem_bytes;
+}
+
+template <typename T, typename TA, typename TB, typename TC>
+cudaError_t gemm(const GemmDesc& d, cudaStream_t stream, void* workspace, size_t ws_bytes, int num_sms) {
+  if (d.M <= 0 || d.N <= 0) return cudaSuccess;
+  const int64_t nb = d.batch1 * d.batch2;
+  if (d.K <= 0) {
+    // C = beta * C (alpha term is empty)
+    GemmDesc z = d;
+    z.K = 0;
+    splitk_reduce_kernel<T, TC><<<std::max<int64_t>(1, std::min<int64_t>(4096, (nb * d.M * d.N + 255) / 256)), 256, 0, stream>>>(z, 0, (const T*)nullptr);
+    count_launch();
+    return cudaGetLastError();
+  }
+  if constexpr (sizeof(T) == 8) {
+    return run<T, CfgF64, TA, TB, TC>(d, stream, workspace, ws_bytes, num_sms);
+  } else {
+    if (use_tall(d)) return run<T, CfgF32Tall, TA, TB, TC>(d, stream, workspace, ws_bytes, num_sms);
+    return run<T, CfgF32, TA, TB, TC>(d, stream, workspace, ws_bytes, num_sms);
+  }
+}
+
 #define CPHF_INST(T, TA, TB, TC) \
   template cudaError_t gemm<T, TA, TB, TC>(const GemmDesc&, cudaStream_t, void*, size_t, int);
 CPHF_INST(double, double, double, double)
@@ -257,5 +351,10 @@ CPHF_INST(float, float, double, double)
 CPHF_INST(float, double, double, float)
 CPHF_INST(float, double, float, double)
 #undef CPHF_INST
+
+cudaError_t gemm_f64_emulated(const GemmDesc& d, cudaStream_t stream, void* workspace, size_t ws_bytes,
+                              int num_sms) {
+  return gemm<dfloat, double, double, double>(d, stream, workspace, ws_bytes, num_sms);
+}
 
 }  // namespace cphf

@@ -28,6 +28,11 @@ struct GemmDesc {
   int64_t batch1 = 1, batch2 = 1;
   int64_t a_b1 = 0, a_b2 = 0, b_b1 = 0, b_b2 = 0, c_b1 = 0, c_b2 = 0;
   double alpha = 1.0, beta = 0.0;
+  // Optional two-level row / column index: with m_div > 0, row m = m0 + m_div * m1 sits at
+  // m0 * a_m + m1 * a_m2 in A and m0 * c_m + m1 * c_m2 in C (likewise n_div for B and C
+  // columns).  Lets a batch of narrow GEMMs run as one tall GEMM.
+  int64_t m_div = 0, a_m2 = 0, c_m2 = 0;
+  int64_t n_div = 0, b_n2 = 0, c_n2 = 0;
 };
 
 enum class Prec { F64, F32 };
@@ -42,5 +47,10 @@ cudaError_t gemm(const GemmDesc& d, cudaStream_t stream, void* workspace = nullp
 
 // Workspace bytes that gemm<> may use for split-K on descriptor d.
 size_t gemm_workspace_bytes(const GemmDesc& d, size_t elem_bytes, int num_sms = 152);
+
+// FP64 operands and result, products and sums in double-float arithmetic on the FP32 pipes
+// (about 2^-46 relative per term; GB300 runs FP32 ~60x faster than FP64).
+cudaError_t gemm_f64_emulated(const GemmDesc& d, cudaStream_t stream, void* workspace = nullptr,
+                              size_t ws_bytes = 0, int num_sms = 152);
 
 }  // namespace cphf

@@ -16,6 +16,7 @@
 #include "kernels.cuh"
 #include "mlp.cuh"
 #include "tc_gemm.cuh"
+#include "xc_grouped.cuh"
 
 namespace cphf {
 
@@ -122,11 +123,12 @@ static void rijk_response_lowp(cphf_ctx* c, float* const* bra, int64_t nb, float
       for (int64_t P0 = 0; P0 < naux; P0 += np_max) {
         const int64_t np = std::min<int64_t>(np_max, naux - P0);
         if (!L.use_tc) {
+          // T[(nu,Pl),(i,a)]: rows (nu, a) two-level, columns i, batch over P
           GemmDesc t;
-          t.M = nao; t.N = no; t.K = no; t.batch1 = np; t.batch2 = nb;
-          t.A = bra[s]; t.a_m = 1; t.a_k = nao; t.a_b1 = 0; t.a_b2 = nao * no;
-          t.B = sp.O32.as<float>() + P0 * no * no; t.b_k = 1; t.b_n = no; t.b_b1 = no * no; t.b_b2 = 0;
-          t.C = L.s_T.p; t.c_m = 1; t.c_n = nao * np; t.c_b1 = nao; t.c_b2 = nao * np * no;
+          t.M = nao * nb; t.N = no; t.K = no; t.batch1 = np;
+          t.A = bra[s]; t.a_m = 1; t.m_div = nao; t.a_m2 = nao * no; t.a_k = nao; t.a_b1 = 0;
+          t.B = sp.O32.as<float>() + P0 * no * no; t.b_k = 1; t.b_n = no; t.b_b1 = no * no;
+          t.C = L.s_T.p; t.c_m = 1; t.c_m2 = nao * np * no; t.c_n = nao * np; t.c_b1 = nao;
           gemm32(c, t);
           GemmDesc k1;
           k1.M = nao; k1.N = no * nb; k1.K = nao * np;
@@ -136,11 +138,14 @@ static void rijk_response_lowp(cphf_ctx* c, float* const* bra, int64_t nb, float
           k1.alpha = -c->scale_k; k1.beta = 1.0;
           gemm32(c, k1);
         }
+        // Wt[(j,Pl),(i,a)] = sum_nu bra[nu, (j,a)] Z_P[nu, i]: rows (j, a) two-level in the
+        // output, columns i, K = nu, batch over P
         GemmDesc w;
-        w.M = no; w.N = no; w.K = nao; w.batch1 = np; w.batch2 = nb;
-        w.A = sp.Z32.as<float>() + P0 * nao * no; w.a_m = nao; w.a_k = 1; w.a_b1 = nao * no; w.a_b2 = 0;
-        w.B = bra[s]; w.b_k = 1; w.b_n = nao; w.b_b1 = 0; w.b_b2 = nao * no;
-        w.C = L.s_W.p; w.c_m = no * np; w.c_n = 1; w.c_b1 = no; w.c_b2 = no * np * no;
+        w.M = no * nb; w.N = no; w.K = nao; w.batch1 = np;
+        w.A = bra[s]; w.a_m = nao; w.a_k = 1; w.a_b1 = 0;
+        w.B = sp.Z32.as<float>() + P0 * nao * no; w.b_k = 1; w.b_n = nao; w.b_b1 = nao * no;
+        w.C = L.s_W.p; w.m_div = no; w.a_m2 = nao * no; w.c_m = 1; w.c_m2 = no * np * no; w.c_n = no * np;
+        w.c_b1 = no;
         gemm32(c, w);
         GemmDesc k2;
         k2.M = nao; k2.N = no * nb; k2.K = no * np;
@@ -159,56 +164,8 @@ static void rijk_response_lowp(cphf_ctx* c, float* const* bra, int64_t nb, float
 
 static void xc_response_lowp(cphf_ctx* c, float* const* bra, int64_t nb, float* const* out, bool accumulate) {
   LowpState& L = *c->lowp;
-  const int ns = c->nspin;
-  const int64_t nao = c->nao;
-  if (!accumulate)
-    for (int s = 0; s < ns; ++s)
-      if (c->spin[s].nocc > 0) CPHF_CUDA(cudaMemsetAsync(out[s], 0, (size_t)nao * c->spin[s].nocc * nb * 4, c->stream));
-  int64_t max_pts = 0;
-  for (const XcBatch& b : c->xc_batches) max_pts = std::max(max_pts, b.npts);
-  int64_t ket_per_spin = 0;
-  for (int s = 0; s < ns; ++s) ket_per_spin = std::max(ket_per_spin, max_pts * c->spin[s].nocc * nb);
-  L.s_ket.ensure((size_t)std::max<int64_t>(1, ket_per_spin * ns) * 4, c->counter());
-  L.s_rho.ensure((size_t)std::max<int64_t>(1, max_pts * nb * 2) * 4, c->counter());
-  const double fac = ns == 1 ? 4.0 : 2.0;
-  float* ket = L.s_ket.as<float>();
-  float* rho = L.s_rho.as<float>();
-  for (const XcBatch& b : c->xc_batches) {
-    if (b.npts == 0 || b.nwin == 0) continue;
-    const float* phi = L.phi32.as<float>() + b.phi_off;
-    for (int s = 0; s < ns; ++s) {
-      const int64_t no = c->spin[s].nocc;
-      float* ket_s = ket + s * ket_per_spin;
-      float* rho_s = rho + s * b.npts * nb;
-      if (no == 0) {
-        CPHF_CUDA(cudaMemsetAsync(rho_s, 0, (size_t)b.npts * nb * 4, c->stream));
-        continue;
-      }
-      GemmDesc d;
-      d.M = b.npts; d.N = no * nb; d.K = b.nwin;
-      d.A = phi; d.a_m = 1; d.a_k = b.npts;
-      d.B = bra[s] + b.lo; d.b_k = 1; d.b_n = nao;
-      d.C = ket_s; d.c_m = 1; d.c_n = b.npts;
-      gemm32(c, d);
-      launch_xc_rho<float>(c->spin[s].aobra32.as<float>() + b.g0, c->ngrids, ket_s, b.npts, no, nb, rho_s,
-                           b.npts, c->stream);
-    }
-    for (int s = 0; s < ns; ++s) {
-      const int64_t no = c->spin[s].nocc;
-      if (no == 0) continue;
-      float* ket_s = ket + s * ket_per_spin;
-      launch_xc_q<float>(c->spin[s].aobra32.as<float>() + b.g0, c->ngrids, c->weights.as<double>() + b.g0,
-                         c->fxc.as<double>() + b.g0, c->ngrids, ns, s, rho, b.npts, b.npts * nb, b.npts, no,
-                         nb, ket_s, c->stream);
-      GemmDesc d;
-      d.M = b.nwin; d.N = no * nb; d.K = b.npts;
-      d.A = phi; d.a_m = b.npts; d.a_k = 1;
-      d.B = ket_s; d.b_k = 1; d.b_n = b.npts;
-      d.C = out[s] + b.lo; d.c_m = 1; d.c_n = nao;
-      d.alpha = fac; d.beta = 1.0;
-      gemm32(c, d);
-    }
-  }
+  const float* aobra[2] = {c->spin[0].aobra32.as<float>(), c->nspin > 1 ? c->spin[1].aobra32.as<float>() : nullptr};
+  xc_response_grouped<float>(c, bra, nb, out, accumulate, L.phi32.as<float>(), aobra, L.s_ket, L.s_rho);
 }
 
 void response_mo_lowp(cphf_ctx* c, const double* x, int64_t nb, double* y) {
@@ -336,7 +293,14 @@ bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, d
     launch_axpby(1.0, dlt, 1.0, x, n * nset, s);
     st->refine_steps += 1;
     if (step == 0 || c->cfg.fp64_every_step) {
-      res = fp64_residual(c, b, x, nset, r, st);
+      c->f64_emulate = c->cfg.residual_dfloat != 0;
+      try {
+        res = fp64_residual(c, b, x, nset, r, st);
+      } catch (...) {
+        c->f64_emulate = false;
+        throw;
+      }
+      c->f64_emulate = false;
       done = res < c->cfg.residual_tol;
     } else {
       response_mo_lowp(c, dlt, nset, adl);

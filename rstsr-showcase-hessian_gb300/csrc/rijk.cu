@@ -22,13 +22,19 @@
 
 namespace cphf {
 
-const char* const kProfNames[PROF_NCLASS] = {"gemm_fp64_simt", "gemm_fp32_simt", "kterm_tcgen05_f16x3"};
+const char* const kProfNames[PROF_NCLASS] = {"gemm_fp64_simt", "gemm_fp32_simt", "kterm_tcgen05_f16x3",
+                                             "gemm_fp64_dfloat"};
 
 static double gemm_flops(const GemmDesc& d) { return 2.0 * d.M * d.N * d.K * d.batch1 * d.batch2; }
 
 void gemm64(cphf_ctx* c, const GemmDesc& d) {
   const size_t need = gemm_workspace_bytes(d, 8, c->num_sms);
   if (need) c->ws_gemm.ensure(need, c->counter());
+  if (c->f64_emulate) {
+    ProfScope ps(c, PROF_GEMM_F64E, gemm_flops(d), 8.0 * (d.M * d.K + d.K * d.N + d.M * d.N) * d.batch1 * d.batch2);
+    CPHF_CUDA(gemm_f64_emulated(d, c->stream, c->ws_gemm.p, c->ws_gemm.bytes, c->num_sms));
+    return;
+  }
   ProfScope ps(c, PROF_GEMM_F64, gemm_flops(d), 8.0 * (d.M * d.K + d.K * d.N + d.M * d.N) * d.batch1 * d.batch2);
   CPHF_CUDA((gemm<double, double, double, double>(d, c->stream, c->ws_gemm.p, c->ws_gemm.bytes, c->num_sms)));
 }

@@ -415,12 +415,13 @@ void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, 
   const int ppc = 16;
   for (int64_t P0 = 0; P0 < naux; P0 += np) {
     const int64_t npc = std::min<int64_t>(np, naux - P0);
-    // T32[Pl][(i,a)][nu] = sum_j bra[nu, j, a] O_P[j, i]
+    // T32[Pl][(i,a)][nu] = sum_j bra[nu, j, a] O_P[j, i]: one tall GEMM per aux function,
+    // rows (nu, a) (two-level index), columns i, K = j
     GemmDesc t;
-    t.M = nao; t.N = no; t.K = no; t.batch1 = npc; t.batch2 = nb;
-    t.A = bra; t.a_m = 1; t.a_k = nao; t.a_b1 = 0; t.a_b2 = nao * no;
-    t.B = O32 + P0 * no * no; t.b_k = 1; t.b_n = no; t.b_b1 = no * no; t.b_b2 = 0;
-    t.C = T32; t.c_m = 1; t.c_n = ldk; t.c_b1 = N * ldk; t.c_b2 = no * ldk;
+    t.M = nao * nb; t.N = no; t.K = no; t.batch1 = npc;
+    t.A = bra; t.a_m = 1; t.m_div = nao; t.a_m2 = nao * no; t.a_k = nao; t.a_b1 = 0;
+    t.B = O32 + P0 * no * no; t.b_k = 1; t.b_n = no; t.b_b1 = no * no;
+    t.C = T32; t.c_m = 1; t.c_m2 = ldk * no; t.c_n = ldk; t.c_b1 = N * ldk;
     gemm32(c, t);
     const int64_t tn = npc * N * ldk;
     CPHF_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned), c->stream));

@@ -117,6 +117,20 @@ def test_xc_response_rks():
     assert rel_err(ctx.get_response_bra(bra), both) < 1e-12
 
 
+@pytest.mark.parametrize("chunk", [900, 2500])
+def test_xc_response_chunked_grouped(chunk):
+    """Uneven per-atom batches split over several chunks of the grouped XC kernels."""
+    s = synth.make_system(GRID_R, seed=15)
+    ctx = make_ctx(s, xc_chunk_points=chunk)
+    bra = np.random.default_rng(15).standard_normal((s.nao, s.nocc[0], 3))
+    g = s.grid
+    ref = xc.rks_response_bra(g.ao, g.weights, g.fxc, bra, s.mo_coeff[0][:, :s.nocc[0]])
+    assert rel_err(ctx.get_response_bra(bra, plugin="xc"), ref) < 1e-12
+    lp = make_ctx(s, precision="mixed", xc_chunk_points=chunk)
+    mo1 = np.random.default_rng(16).standard_normal((s.nao, s.nocc[0], 3))
+    assert rel_err(lp.response_dimless_cphf_lowp(mo1), ctx.response_dimless_cphf(mo1)) < 3e-6
+
+
 def test_xc_response_uks():
     s = synth.make_system(GRID_U, seed=6)
     ctx = make_ctx(s)
