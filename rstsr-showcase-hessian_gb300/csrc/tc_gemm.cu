@@ -271,11 +271,12 @@ __global__ void split_cderi_kernel(const double* __restrict__ Bd, int64_t nao, i
 }
 
 // |x| maxima: one atomicMax on the float bit pattern per block
-__global__ void absmax_f32_kernel(const float* __restrict__ x, int64_t n, int64_t row, int64_t valid,
+// max |x| over rows [0, rows) of length `valid` with row stride `ld` (no per-element division)
+__global__ void absmax_f32_kernel(const float* __restrict__ x, int64_t rows, int64_t ld, int64_t valid,
                                   unsigned* out) {
   float m = 0.f;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
-    if (t % row < valid) m = fmaxf(m, fabsf(x[t]));
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x)
+    for (int64_t v = threadIdx.x; v < valid; v += blockDim.x) m = fmaxf(m, fabsf(x[r * ld + v]));
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
 }
@@ -425,7 +426,8 @@ void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, 
     gemm32(c, t);
     const int64_t tn = npc * N * ldk;
     CPHF_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned), c->stream));
-    absmax_f32_kernel<<<grid_for(tn), 256, 0, c->stream>>>(T32, tn, ldk, nao, mx);
+    absmax_f32_kernel<<<(unsigned)std::min<int64_t>(npc * N, 8 * (int64_t)c->num_sms), 256, 0, c->stream>>>(
+        T32, npc * N, ldk, nao, mx);
     t_scale_kernel<<<1, 1, 0, c->stream>>>(mx, (float)L.sA, (float)alpha, scale);
     split_t_kernel<<<grid_for(tn), 256, 0, c->stream>>>(T32, tn, scale, Thi.as<__half>(), Tlo.as<__half>());
     count_launch(3);

@@ -226,13 +226,13 @@ def test_lowp_operator_accuracy(dims, tc):
         assert rel_err(a, b) < 3e-6
 
 
-@pytest.mark.parametrize("dims", [MEDIUM, GRID_U, TC_RAGGED])
-def test_mixed_precision_solve(dims):
+@pytest.mark.parametrize("dims,dfloat", [(MEDIUM, 1), (MEDIUM, 0), (GRID_U, 1), (TC_RAGGED, 1)])
+def test_mixed_precision_solve(dims, dfloat):
     s = synth.make_system(dims, seed=13)
     rhs = s.rhs[0] if s.nspin == 1 else s.rhs
     c64 = make_ctx(s, cphf_tol=1e-10, cphf_lindep=1e-20)
     x64 = c64.solve_dimless_cphf(rhs)
-    cmx = make_ctx(s, precision="mixed")
+    cmx = make_ctx(s, precision="mixed", residual_dfloat=dfloat)
     xmx = cmx.solve_dimless_cphf(rhs)
     st = cmx.last_stats
     assert st["residual_max"] < 1e-8
