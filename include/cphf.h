@@ -205,6 +205,23 @@ cphf_status cphf_dense_op_destroy(cphf_dense_op* op);
 /* Copy `bytes` between any host / device pointers on the context's stream and wait. */
 cphf_status cphf_copy(cphf_ctx* ctx, void* dst, const void* src, int64_t bytes);
 
+/* ---- allocation-free RI-J response (no counterpart in the reference) -------------------- */
+/* For callers that cannot allocate device memory (code running under another framework's
+ * allocator or memory budget, or recording work where allocation is not allowed): the
+ * Coulomb part of the RI-JK response in bra form, out = scale_j * J[D1] Cocc, computed with
+ * no cudaMalloc, no cudaFree and no allocating library call, and without a context.
+ *   Z   [nao, nocc, naux]  Z_P = B_P Cocc (device)
+ *   bra [nao, nocc, nb], out [nao, nocc, nb] (device), FP64 col-major; stream: a cudaStream_t or NULL.
+ * The one intermediate, d[naux, nb], lives in a static 8 MiB device array of the library:
+ * naux * nb must not exceed cphf_rij_noalloc_capacity() (1,048,576), else CPHF_ERR_ARG is
+ * returned and nothing runs.  The first call on a device resolves that array's device
+ * address (cudaGetSymbolAddress) with the device current; make that first call before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU (different
+ * streams, or different host threads on one device) race and must be serialized by the caller. */
+int64_t cphf_rij_noalloc_capacity(void);
+cphf_status cphf_rij_response_bra_noalloc(const double* Z, const double* bra, int64_t nao, int64_t nocc,
+                                          int64_t naux, int64_t nb, double scale_j, double* out,
+                                          void* stream);
 
 /* ---- learned initial guess / preconditioner (no counterpart in the reference) ------------ */
 /* Per-(i,a)-pair MLP 3 -> 64 -> 64 -> 2 (GELU), FP32 weights packed as

@@ -36,7 +36,8 @@ EXPORTS = [
     "cphf_get_cphf_hess", "cphf_krylov_block", "cphf_dense_op_create", "cphf_dense_op_apply",
     "cphf_dense_op_destroy", "cphf_copy", "cphf_mlp_set_weights", "cphf_ctx_tensor_cores_active",
     "cphf_ctx_profile", "cphf_ctx_profile_report", "cphf_mlp_get_weights", "cphf_mlp_features",
-    "cphf_mlp_forward", "cphf_mlp_loss_grad", "cphf_mlp_train",
+    "cphf_mlp_forward", "cphf_mlp_loss_grad", "cphf_mlp_train", "cphf_rij_noalloc_capacity",
+    "cphf_rij_response_bra_noalloc",
 ]
 MLP_NWEIGHTS = 4546
 
