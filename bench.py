@@ -52,8 +52,13 @@ def parse():
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison solve")
     p.add_argument("--cpu-sample", type=int, default=12, help="RHS columns of the CPU baseline sample")
     p.add_argument("--no-learned", action="store_true", help="do not use the trained initial guess")
-    p.add_argument("--fp64-tol", type=float, default=1e-10,
-                   help="Krylov tol of the plain FP64 solve (tight enough for a verified ||r|| < 1e-8)")
+    p.add_argument("--fp64-tol", type=float, default=1e-10, help="Krylov tol of the plain FP64 solve")
+    p.add_argument("--fp64-lindep", type=float, default=1e-20,
+                   help="Krylov lindep of the plain FP64 solve; the convergence test is max(lindep, tol^2), "
+                        "so the default 1e-14 would stop it above the ||r|| < 1e-8 target")
+    p.add_argument("--residual", type=int, default=2, choices=[0, 1, 2],
+                   help="mixed solve's correction residual: 0 FP64, 1 double-float, 2 double-float + "
+                        "tensor-core K term with exact BF16 slices")
     return p.parse_args()
 
 
@@ -237,7 +242,8 @@ def run_gpu(args, world, rank, local):
 
     weights = ROOT / "rstsr-showcase-hessian_gb300" / "cphf_gb300" / "mlp_weights.npy"
     learned = weights.exists() and not args.no_learned and nspin == 1
-    mixed = make_ctx("mixed", verify_residual=0, use_learned_guess=1 if learned else 0)
+    mixed = make_ctx("mixed", verify_residual=0, use_learned_guess=1 if learned else 0,
+                     residual_dfloat=args.residual)
     if learned:
         mixed.set_mlp_weights(np.load(weights))
     # device-resident inputs and outputs (F-contiguous views of C-ordered tensors)
@@ -285,7 +291,7 @@ def run_gpu(args, world, rank, local):
     x_mixed = [o.numpy().transpose(3, 2, 1, 0).copy(order="F") for o in out_p]
 
     # plain FP64 solve of the same system (the reference's arithmetic), timed once
-    fp64 = make_ctx("fp64", cphf_tol=args.fp64_tol)
+    fp64 = make_ctx("fp64", cphf_tol=args.fp64_tol, cphf_lindep=args.fp64_lindep)
     fp64_res = None
     if not args.no_fp64:
         t = time.perf_counter()
@@ -320,6 +326,10 @@ def run_gpu(args, world, rank, local):
         peak = measure_fp64_peak()
         roof = dict(bound="tensor", achieved=dom["flops"] / dom["ms"] / 1e9, peak=peak, unit="TFLOP/s",
                     peak_source="in-run cuBLAS FP64 GEMM 8192^3 (FP64 has no entry in MEASURED_PEAKS.json)")
+    elif dom_name == "kterm_tcgen05_bf16x6_exact":
+        roof = dict(bound="tensor", achieved=dom["flops"] / dom["ms"] / 1e9, peak=bf16, unit="TFLOP/s",
+                    peak_source=f"{peak_src} bf16 dense; achieved counts the algorithmic FP64 FLOPs, the "
+                                "tensor pipe executes 21 BF16 slice products")
     elif dom_name == "kterm_tcgen05_f16x3":
         roof = dict(bound="tensor", achieved=dom["flops"] / dom["ms"] / 1e9, peak=bf16, unit="TFLOP/s",
                     peak_source=f"{peak_src} bf16 dense (FP16 runs at the same rate); achieved counts "
@@ -336,14 +346,17 @@ def run_gpu(args, world, rank, local):
     line = dict(
         metric=METRIC, value=t_step, unit="s", n_gpus=args.gpus, steps=args.steps, warmup=args.warmup,
         ms_per_step=t_step * 1e3, higher_is_better=False, scaling="weak", vs_baseline=None,
-        dtype="f16x3 tensor-core operator / f32 / f64 defect correction",
+        dtype=("f16x3 tensor-core operator / f32 / f64 defect correction"
+               + {0: " (fp64 residual)", 1: " (double-float residual)",
+                  2: " (residual: bf16x6 exact-slice tensor-core K term + double-float)"}[args.residual]),
         data=f"synthetic (seeded generator, {args.workload}, seed {args.seed})",
         config=dict(workload=args.workload, description=WORKLOAD_DESC.get(args.workload, args.workload),
-                    precision="mixed", learned_guess=learned,
+                    precision="mixed", learned_guess=learned, residual_mode=args.residual,
                     parallelism="replicas" if world > 1 else "single GPU",
                     l2="inputs larger than L2 (dense cderi FP64 %.1f GB)" % (s.nao ** 2 * s.naux * 8 / 1e9)),
         fp64_plain=None if args.no_fp64 else dict(value=t_fp64, unit="s", aop_calls=st64["aop_calls"],
-                                                  cycles=st64["cycles"], tol=args.fp64_tol),
+                                                  cycles=st64["cycles"], tol=args.fp64_tol,
+                                                  lindep=args.fp64_lindep),
         speedup_vs_fp64_plain=None if args.no_fp64 else t_fp64 / t_step,
         residual=dict(mixed_verified=res_mixed, fp64_plain_verified=fp64_res, target=1e-8),
         hessian_max_abs_diff_vs_fp64=hess_diff,

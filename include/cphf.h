@@ -45,7 +45,7 @@ typedef enum cphf_status {
 /* Arithmetic of the solve. */
 typedef enum cphf_precision {
   CPHF_PRECISION_FP64 = 0,   /* every contraction in FP64 (the reference's arithmetic) */
-  CPHF_PRECISION_MIXED = 1   /* split-BF16 tensor-core operator inside FP64 defect correction */
+  CPHF_PRECISION_MIXED = 1   /* split-FP16 tensor-core operator inside FP64 defect correction */
 } cphf_precision;
 
 /* HessSCFConfig (src/hessian/rscf.rs:5-18) plus the GPU-side options. */
@@ -67,9 +67,11 @@ typedef struct cphf_config {
   int32_t verify_residual;   /* mixed: recompute the final residual with the FP64 operator (default 1) */
   int32_t fp64_every_step;   /* mixed: FP64 residual after every correction, not only the first (default 0) */
   int64_t xc_chunk_points;   /* grid points per XC chunk (default 0 = 8 GiB of intermediates) */
-  int32_t residual_dfloat;   /* mixed: the correction residuals in double-float arithmetic on the FP32
-                                pipes (~1e-14 relative, default 1); 0 = native FP64.  The final
-                                verification (verify_residual) is always native FP64. */
+  int32_t residual_dfloat;   /* mixed: arithmetic of the correction residuals.  0 = native FP64;
+                                1 = double-float GEMMs on the FP32 pipes (~1e-14 relative, default);
+                                2 = as 1, with the RI-K term B_P bra O_P on the tensor cores as exact
+                                BF16 slice products (6 x 6 bits, ~1e-10 relative to sum |B||T|).
+                                The final verification (verify_residual) is always native FP64. */
 } cphf_config;
 
 /* Solver statistics (the reference reports them by println!, krylov_block.rs:148-151, 175). */

@@ -14,11 +14,22 @@ struct cphf_ctx;
 
 namespace cphf {
 
+// Slice copies and scratch of the FP64-accurate tensor-core K term (tc_ozaki.cu).
+struct OzState {
+  DevBuf A;                    // [6][naux][nao][ldk] BF16 slices of the row-scaled cderi
+  DevBuf rowscale, e_row, mx;  // per-row power-of-two scales of A
+  DevBuf T, B;                 // FP64 T chunk [np][N][ldk] and its 6 BF16 slices
+  DevBuf colscale, e_col, mxc, err;
+  int64_t ldk = 0;
+  bool ready = false;
+};
+
 // State of the split-precision operator (mixed.cu).
 struct LowpState {
   DevBuf Bd32;                 // [nao, nao, naux] FP32 (SIMT fallback of the K term)
-  DevBuf Bhi, Blo;             // BF16 hi / lo split of the dense cderi for the tensor-core K term
-  int64_t ldk = 0;             // padded row length of the BF16 copies
+  DevBuf Bhi, Blo;             // FP16 hi / lo split of the dense cderi for the tensor-core K term
+  int64_t ldk = 0;             // padded row length of the FP16 copies
+  OzState oz;                  // FP64-accurate tensor-core K term of the residual
   DevBuf phi32;
   DevBuf s_c1, s_resp, s_T, s_W, s_d, s_ket, s_rho, s_y, s_x, s_Thi, s_Tlo, s_acc;
   DevBuf err;                  // device error flag of the tensor-core kernels (bounded waits)
@@ -96,7 +107,14 @@ struct Profiler {
     for (auto e : pool) cudaEventDestroy(e);
   }
 };
-enum ProfClass { PROF_GEMM_F64 = 0, PROF_GEMM_F32 = 1, PROF_TC_KTERM = 2, PROF_GEMM_F64E = 3, PROF_NCLASS = 4 };
+enum ProfClass {
+  PROF_GEMM_F64 = 0,
+  PROF_GEMM_F32 = 1,
+  PROF_TC_KTERM = 2,
+  PROF_GEMM_F64E = 3,
+  PROF_TC_OZAKI = 4,
+  PROF_NCLASS = 5
+};
 extern const char* const kProfNames[PROF_NCLASS];
 
 }  // namespace cphf
@@ -140,6 +158,7 @@ struct cphf_ctx {
   std::unique_ptr<cphf::MlpState> mlp;
   cphf::Profiler prof;
   bool f64_emulate = false;  // route the FP64 GEMMs through the double-float kernel
+  bool oz_kterm = false;     // FP64 K term 1 on the tensor cores (exact BF16 slices)
 
   int64_t* counter() { return &device_bytes; }
 };

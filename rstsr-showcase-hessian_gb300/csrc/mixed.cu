@@ -2,7 +2,7 @@
 //
 // The operator is the same sequence of contractions as the FP64 path (rijk.cu, xc.cu,
 // operator.cu) with FP32 operands and accumulation; the dominant K-term contraction
-// B_P bra O_P runs on the tensor cores as a three-product split-BF16 GEMM with FP32
+// B_P bra O_P runs on the tensor cores as a three-product split-FP16 GEMM with FP32
 // accumulation in TMEM (tc_gemm.cu).  Its error (~1e-6 relative) is removed by defect
 // correction: each step solves (I + A_lowp) d = r with the device Krylov solver (FP64
 // basis, orthogonalisation and projected solve), then recomputes r = b - (I + A) x with
@@ -16,6 +16,7 @@
 #include "kernels.cuh"
 #include "mlp.cuh"
 #include "tc_gemm.cuh"
+#include "tc_ozaki.cuh"
 #include "xc_grouped.cuh"
 
 namespace cphf {
@@ -294,13 +295,16 @@ bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, d
     st->refine_steps += 1;
     if (step == 0 || c->cfg.fp64_every_step) {
       c->f64_emulate = c->cfg.residual_dfloat != 0;
+      c->oz_kterm = c->cfg.residual_dfloat == 2 && c->has_rijk && c->lowp->use_tc && oz_available(c);
       try {
         res = fp64_residual(c, b, x, nset, r, st);
       } catch (...) {
         c->f64_emulate = false;
+        c->oz_kterm = false;
         throw;
       }
       c->f64_emulate = false;
+      c->oz_kterm = false;
       done = res < c->cfg.residual_tol;
     } else {
       response_mo_lowp(c, dlt, nset, adl);

@@ -30,9 +30,11 @@
 
 #include "kernels.cuh"
 #include "tc_gemm.cuh"
+#include "tc_ptx.cuh"
 
 namespace cphf {
 namespace {
+using namespace tcx;
 
 constexpr int BM = 128, BN = 256, BK = 64;
 constexpr int STAGES = 2;
@@ -41,85 +43,6 @@ constexpr int B_TILE = BN * BK * 2;
 constexpr int STAGE_BYTES = 2 * A_TILE + 2 * B_TILE;  // hi + lo planes of both operands
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*barriers*/ + 1024 /*alignment*/;
 constexpr int TMEM_COLS = 256;
-constexpr uint32_t WAIT_LIMIT = 1u << 26;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-// Bounded parity wait; returns false (and raises *err) when the limit is reached.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err) {
-  for (uint32_t i = 0; i < WAIT_LIMIT; ++i) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (ok) return true;
-    if ((i & 1023) == 1023 && *(volatile int*)err) return false;
-  }
-  atomicExch(err, 1);
-  return false;
-}
-
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int c0, int c1,
-                                            int c2) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1), "r"(c2)
-      : "memory");
-}
-
-// Shared-memory matrix descriptor: K-major operand, 128B swizzle, 8-row groups 1024 B apart.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
-  d |= (uint64_t)1 << 16;             // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset: 8 rows x 128 B
-  d |= (uint64_t)1 << 46;             // descriptor version for tcgen05
-  d |= (uint64_t)2 << 61;             // SWIZZLE_128B
-  return d;
-}
-
-// Instruction descriptor: kind::f16, A/B FP16, D FP32, K-major A and B, M = 128, N = 256.
-__host__ __device__ constexpr uint32_t instr_desc() {
-  return (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(idesc), "r"(acc)
-      : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
 
 struct TcArgs {
   float* out;
@@ -190,21 +113,19 @@ __global__ void __launch_bounds__(128, 1)
       }
       // drain: the copies of the last round of every stage have landed before the CTA may exit
       for (int it = max(0, issued - STAGES); it < issued; ++it) {
-        int dummy = 0;
-        mbar_wait(full0 + 8 * (it % STAGES), (it / STAGES) & 1, &dummy);
+        mbar_wait(full0 + 8 * (it % STAGES), (it / STAGES) & 1, nullptr);
       }
     } else if (warp == 1 && lane == 0) {
       // MMA issuer
-      constexpr uint32_t idesc = instr_desc();
-      bool ok = true;
+      constexpr uint32_t idesc = instr_desc_f16(BM, BN, false);
       for (int it = 0; it < total; ++it) {
         const int s = it % STAGES;
         const uint32_t ph = (it / STAGES) & 1;
-        if (!mbar_wait(full0 + 8 * s, ph, args.err)) { ok = false; break; }
+        if (!mbar_wait(full0 + 8 * s, ph, args.err)) break;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
-        const uint64_t ah = smem_desc(st), al = smem_desc(st + A_TILE);
-        const uint64_t bh = smem_desc(st + 2 * A_TILE), bl = smem_desc(st + 2 * A_TILE + B_TILE);
+        const uint64_t ah = smem_desc<128>(st), al = smem_desc<128>(st + A_TILE);
+        const uint64_t bh = smem_desc<128>(st + 2 * A_TILE), bl = smem_desc<128>(st + 2 * A_TILE + B_TILE);
 #pragma unroll
         for (int k = 0; k < BK / 16; ++k) {
           const uint64_t dk = (uint64_t)((k * 32) >> 4);  // 16 FP16 = 32 B along K inside the swizzle atom
@@ -214,7 +135,6 @@ __global__ void __launch_bounds__(128, 1)
         }
         mma_commit(empty0 + 8 * s);
       }
-      (void)ok;
       mma_commit(accum);  // also covers an early exit: arrives when the issued MMAs retire
     }
     __syncwarp();

@@ -1,6 +1,6 @@
-// Tensor-core (tcgen05 / TMEM / TMA) split-BF16 contraction of the RI-K term
+// Tensor-core (tcgen05 / TMEM / TMA) split-FP16 contraction of the RI-K term
 //   out[mu, (i,a)] += alpha * sum_P sum_nu B_P[mu,nu] T_P[nu,(i,a)],   T_P = bra_a O_P
-// (src/ri_jk/hess_r.rs:168-170), with B and T each split into BF16 hi + lo and the three
+// (src/ri_jk/hess_r.rs:168-170), with B and T each split into FP16 hi + lo and the three
 // products hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory.
 #pragma once
 #include <cstdint>
@@ -11,7 +11,7 @@ namespace cphf {
 
 // true when the tensor-core path can run on the context's device (sm_103 / sm_100 family)
 bool tc_available(cphf_ctx* c);
-// BF16 hi/lo copies of the dense cderi, rows of length ldk (K-major for the MMA)
+// FP16 hi/lo copies of the dense cderi, rows of length ldk (K-major for the MMA)
 void tc_prepare_cderi(cphf_ctx* c, DevBuf& hi, DevBuf& lo, int64_t& ldk);
 // out (FP32 [nao, nocc, nb]) += alpha * sum_P B_P bra O_P; bra FP32 [nao, nocc, nb], O32 [nocc, nocc, naux]
 void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, const float* O32,

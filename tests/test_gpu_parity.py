@@ -226,7 +226,38 @@ def test_lowp_operator_accuracy(dims, tc):
         assert rel_err(a, b) < 3e-6
 
 
-@pytest.mark.parametrize("dims,dfloat", [(MEDIUM, 1), (MEDIUM, 0), (GRID_U, 1), (TC_RAGGED, 1)])
+def _max_col_residual(c64, s, x):
+    """max_j ||b_j - (I + A) x_j||_2 with the native FP64 operator."""
+    rhs = [s.rhs[0]] if s.nspin == 1 else s.rhs
+    xs = [x] if s.nspin == 1 else x
+    y = c64.response_dimless_cphf(x)
+    y = [y] if s.nspin == 1 else y
+    r = np.concatenate([(b - a - yy).reshape(-1, b.shape[2] * b.shape[3], order="F")
+                        for b, a, yy in zip(rhs, xs, y)], axis=0)
+    return float(np.linalg.norm(r, axis=0).max()), float(max(np.abs(a).max() for a in xs))
+
+
+@pytest.mark.parametrize("dims", [MEDIUM, TC_RAGGED, MEDIUM_U])
+@pytest.mark.parametrize("mode", [1, 2])
+def test_emulated_fp64_residual(dims, mode):
+    """The residual of the mixed solve's first correction, computed with the emulated FP64
+    operator (mode 1: double-float GEMMs; mode 2: plus the K term on the tensor cores with
+    exact BF16 slices, chunked over aux functions), matches the native FP64 residual of the
+    same x to 1e-9 relative to max |x| (the split-FP16 operator of the inner solves is ~1e-6)."""
+    s = synth.make_system(dims, seed=15)
+    rhs = s.rhs[0] if s.nspin == 1 else s.rhs
+    c64 = make_ctx(s)
+    cmx = make_ctx(s, precision="mixed", residual_dfloat=mode, max_refine=1, residual_tol=1.0, verify_residual=0,
+                   aux_chunk=16)
+    x = cmx.solve_dimless_cphf(rhs)
+    res_emul = cmx.last_stats["residual_max"]
+    res_64, xmax = _max_col_residual(c64, s, x)
+    assert 1e-9 < res_64 < 1e-3            # a real, unconverged residual of the low-precision step
+    assert abs(res_emul - res_64) < 1e-9 * max(1.0, xmax), (res_emul, res_64, xmax)
+
+
+@pytest.mark.parametrize("dims,dfloat", [(MEDIUM, 1), (MEDIUM, 0), (GRID_U, 1), (TC_RAGGED, 1), (MEDIUM, 2),
+                                         (TC_RAGGED, 2), (GRID_U, 2)])
 def test_mixed_precision_solve(dims, dfloat):
     s = synth.make_system(dims, seed=13)
     rhs = s.rhs[0] if s.nspin == 1 else s.rhs
