@@ -14,11 +14,21 @@ struct cphf_ctx;
 
 namespace cphf {
 
-// Slice copies and scratch of the FP64-accurate tensor-core K term (tc_ozaki.cu).
+// Per-spin slice copies of the FP64-accurate tensor-core K term (tc_ozaki.cu); every slice
+// array holds 6 BF16 planes, rows scaled by a power of two (exponents alongside).
+struct OzSpin {
+  DevBuf O, eO;        // [6][naux][nocc(i)][ldj] of O_P[j, i], K = j; exponent per (P, i)
+  DevBuf Z, eZ;        // [6][naux][nocc(i)][ldk] of Z_P[nu, i], K = nu; exponent per (P, i)
+  DevBuf Zt, sZt, eZt; // [6][naux][nao(mu)][ldj] of Z_P[mu, j], K = j; scale per mu over (j, P)
+  int64_t ldj = 0;     // padded K = nocc rows
+  bool ready = false;
+};
 struct OzState {
-  DevBuf A;                    // [6][naux][nao][ldk] BF16 slices of the row-scaled cderi
+  DevBuf A;                    // [6][naux][nao][ldk] slices of the row-scaled cderi
   DevBuf rowscale, e_row, mx;  // per-row power-of-two scales of A
-  DevBuf T, B;                 // FP64 T chunk [np][N][ldk] and its 6 BF16 slices
+  OzSpin spin[2];
+  // per-call scratch: bra slices (both K orders), T / Wt staging (FP32 pairs) and slices
+  DevBuf braw, ebraw, brat, ebrat, T, B, W, Ws;
   DevBuf colscale, e_col, mxc, err;
   int64_t ldk = 0;
   bool ready = false;

@@ -295,7 +295,8 @@ bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, d
     st->refine_steps += 1;
     if (step == 0 || c->cfg.fp64_every_step) {
       c->f64_emulate = c->cfg.residual_dfloat != 0;
-      c->oz_kterm = c->cfg.residual_dfloat == 2 && c->has_rijk && c->lowp->use_tc && oz_available(c);
+      c->oz_kterm = c->cfg.residual_dfloat == 2 && c->has_rijk && c->lowp->use_tc && oz_available(c) &&
+                    oz_supported(c);
       try {
         res = fp64_residual(c, b, x, nset, r, st);
       } catch (...) {

@@ -129,34 +129,33 @@ void rijk_response_fp64(cphf_ctx* c, const double* const* bra, int64_t nb, doubl
       const SpinState& sp = c->spin[s];
       const int64_t no = sp.nocc;
       if (no == 0) continue;
-      // term 1 on the tensor cores with exact BF16 slices (FP64-accurate residual of the mixed solve)
-      const bool oz = c->oz_kterm && c->lowp;
-      if (oz) {
+      // the whole K term on the tensor cores with exact BF16 slices (FP64-accurate residual of
+      // the mixed solve)
+      if (c->oz_kterm && c->lowp) {
         if (!written[s]) CPHF_CUDA(cudaMemsetAsync(out[s], 0, (size_t)nao * no * nb * 8, c->stream));
         written[s] = true;
-        oz_k_term1(c, c->lowp->oz, bra[s], sp.O.as<double>(), no, nb, -c->scale_k, out[s]);
+        oz_k_terms(c, c->lowp->oz, s, bra[s], nb, -c->scale_k, out[s]);
+        continue;
       }
       const int64_t np_max = k_chunk(c, no, nb);
-      if (!oz) c->s_T.ensure((size_t)nao * np_max * no * nb * 8, c->counter());
+      c->s_T.ensure((size_t)nao * np_max * no * nb * 8, c->counter());
       c->s_W.ensure((size_t)no * np_max * no * nb * 8, c->counter());
       for (int64_t P0 = 0; P0 < naux; P0 += np_max) {
         const int64_t np = std::min<int64_t>(np_max, naux - P0);
-        if (!oz) {
-          GemmDesc t;  // T[(nu,Pl),(i,a)] = sum_j bra[nu,j,a] O_P[j,i]
-          t.M = nao; t.N = no; t.K = no; t.batch1 = np; t.batch2 = nb;
-          t.A = bra[s]; t.a_m = 1; t.a_k = nao; t.a_b1 = 0; t.a_b2 = nao * no;
-          t.B = sp.O.as<double>() + P0 * no * no; t.b_k = 1; t.b_n = no; t.b_b1 = no * no; t.b_b2 = 0;
-          t.C = c->s_T.p; t.c_m = 1; t.c_n = nao * np; t.c_b1 = nao; t.c_b2 = nao * np * no;
-          gemm64(c, t);
-          GemmDesc k1;  // out += -scale_k Bdense[mu,(nu,P)] T[(nu,P),(i,a)]
-          k1.M = nao; k1.N = no * nb; k1.K = nao * np;
-          k1.A = c->Bd.as<double>() + P0 * nao * nao; k1.a_m = 1; k1.a_k = nao;
-          k1.B = c->s_T.p; k1.b_k = 1; k1.b_n = nao * np;
-          k1.C = out[s]; k1.c_m = 1; k1.c_n = nao;
-          k1.alpha = -c->scale_k; k1.beta = written[s] ? 1.0 : 0.0;
-          gemm64(c, k1);
-          written[s] = true;
-        }
+        GemmDesc t;  // T[(nu,Pl),(i,a)] = sum_j bra[nu,j,a] O_P[j,i]
+        t.M = nao; t.N = no; t.K = no; t.batch1 = np; t.batch2 = nb;
+        t.A = bra[s]; t.a_m = 1; t.a_k = nao; t.a_b1 = 0; t.a_b2 = nao * no;
+        t.B = sp.O.as<double>() + P0 * no * no; t.b_k = 1; t.b_n = no; t.b_b1 = no * no; t.b_b2 = 0;
+        t.C = c->s_T.p; t.c_m = 1; t.c_n = nao * np; t.c_b1 = nao; t.c_b2 = nao * np * no;
+        gemm64(c, t);
+        GemmDesc k1;  // out += -scale_k Bdense[mu,(nu,P)] T[(nu,P),(i,a)]
+        k1.M = nao; k1.N = no * nb; k1.K = nao * np;
+        k1.A = c->Bd.as<double>() + P0 * nao * nao; k1.a_m = 1; k1.a_k = nao;
+        k1.B = c->s_T.p; k1.b_k = 1; k1.b_n = nao * np;
+        k1.C = out[s]; k1.c_m = 1; k1.c_n = nao;
+        k1.alpha = -c->scale_k; k1.beta = written[s] ? 1.0 : 0.0;
+        gemm64(c, k1);
+        written[s] = true;
         GemmDesc w;  // Wt[(j,Pl),(i,a)] = sum_nu Z_P[nu,i] bra[nu,j,a]
         w.M = no; w.N = no; w.K = nao; w.batch1 = np; w.batch2 = nb;
         w.A = sp.Z.as<double>() + P0 * nao * no; w.a_m = nao; w.a_k = 1; w.a_b1 = nao * no; w.a_b2 = 0;

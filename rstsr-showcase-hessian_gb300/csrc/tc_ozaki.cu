@@ -1,31 +1,36 @@
-// FP64-accurate RI-K term 1 on the tensor cores (sm_103a): exact-slice BF16 products
+// FP64-accurate RI-K term on the tensor cores (sm_103a): exact-slice BF16 products
 // accumulated in TMEM (an Ozaki-type splitting), for the FP64 residual of the mixed solve.
 //
-//   out[mu, n] += alpha * sum_P sum_nu B_P[mu, nu] T_P[nu, n],   T_P[nu, (i,a)] = sum_j bra[nu,j,a] O_P[j,i]
+// The exchange response K_s = -sum_P [B_P bra O_P + Z_P (Z_P^T bra)^T] (src/ri_jk/hess_r.rs:
+// 159-176) is evaluated per chunk of aux functions as four contractions, all on tcgen05:
+//   T-gen   T_P[nu, (i,a)] = sum_j bra[nu, j, a] O_P[j, i]        batched over P, K = j
+//   term 1  out[mu, n]   += alpha sum_{P,nu} B_P[mu, nu] T_P[nu, n]  K = (P, nu), split over CTAs
+//   W-gen   W_P[j, (i,a)] = sum_nu bra[nu, j, a] Z_P[nu, i]       batched over P, K = nu
+//   term 2  out[mu, n]   += alpha sum_{P,j} Z_P[mu, j] W_P[j, n]   K = (P, j), split over CTAs
+// with A[m, k] B[n, k] operands stored K-major.
 //
-// (term 1 of the exchange response, src/ri_jk/hess_r.rs:168-170).
-//
-// Slicing.  Each row mu of B (over all nu, P) and each column n of T (over nu and the P of a
-// chunk) is scaled by a power of two so that |v| < 1, then cut into S = 6 slices of 6 bits,
-//   v = sum_t q_t 2^(-6(t+1)) + r,   q_0 in [-64, 64], q_t in [-32, 32] (t > 0), |r| <= 2^-37,
-// with q_t = rint(2^6 (remainder)); every slice is an integer of at most 7 bits times a
-// power of two and is exact in BF16.  The product v_A v_B is approximated by the 21 slice
-// products with t + u <= 5 (dropped terms and remainders ~2^-34 relative).
+// Slicing.  Each operand row (over its K range) is scaled by a power of two 2^-e so that
+// |v| < 1, rounded to the 36-bit fixed-point integer F = round(v 2^36) and cut into six
+// balanced base-64 digits, F = sum_t q_t 2^(30 - 6t), q_0 in [-64, 64], q_t in [-32, 32];
+// slice t = q_t 2^(-6(t+1)) is exact in BF16.  The product is approximated by the 21 slice
+// products with t + u <= 5 (dropped terms and rounding ~2^-34 relative to |row max| x
+// |column max|).  All slicing is integer arithmetic on the FP64 / FP32 bit patterns.
 //
 // Exact accumulation.  A slice product q_t q_u 2^(-6(t+u+2)) is a multiple of 2^(-6(g+2)),
 // g = t + u.  Groups g = 0, 1, 2 each get their own TMEM accumulator; over the K range of
 // one CTA (at most KMAX = 3072 terms) their integer sums stay below 2^24 (g0: 64*64*K,
 // g1: 2*64*32*K, g2: (2*64*32 + 32*32)*K), so the FP32 accumulation is exact.  Groups 3-5
-// share a fourth accumulator whose FP32 rounding is ~2^-24 of a term of size 2^-18.
-// The epilogue adds the four accumulators in FP64, applies alpha * 2^(eA_mu + eT_n) and
-// atomically adds into the FP64 output (split over K ranges across CTAs).
+// share a fourth accumulator whose FP32 rounding is ~2^-24 of a term of size 2^-18.  The
+// epilogue adds the four accumulators as an FP32 pair (two-sum), then either atomically
+// adds alpha 2^(eA + eB) (hi + lo) into the FP64 output (terms 1 and 2, split over K ranges
+// across CTAs) or stores the pair 2^(eA + eB) (hi, lo) into a staging array (T, W).
 //
-// Kernel structure (one CTA per SM, 4 warps, 194 KB shared memory):
-//   warp 0 lane 0  -- TMA producer: 3-D tiled loads of the 6 + 6 slice tiles (K = nu, 32
-//                     wide, 64B swizzle) into a 2-stage ring;
-//   warp 1 lane 0  -- MMA issuer: 21 x tcgen05.mma.kind::f16 (BF16, M=128, N=128, K=16)
-//                     per K step into 4 accumulators (4 x 128 TMEM columns);
-//   warp 2         -- TMEM allocation (512 columns) and release;
+// Kernel structure (one CTA per SM, 4 warps):
+//   warp 0 lane 0  -- TMA producer: 3-D tiled loads of the 6 + 6 slice tiles (K = 32 wide,
+//                     64B swizzle) into a 2-stage ring;
+//   warp 1 lane 0  -- MMA issuer: 21 x tcgen05.mma.kind::f16 (BF16, M=128, N=BN, K=16)
+//                     per K step into 4 accumulators (4 x BN TMEM columns);
+//   warp 2         -- TMEM allocation and release;
 //   warps 0-3      -- epilogue.
 // Every mbarrier wait is bounded; on expiry the kernel raises the error flag and returns.
 #include <cuda.h>
@@ -44,46 +49,79 @@ namespace cphf {
 namespace {
 using namespace tcx;
 
-constexpr int S = 6;          // slices per operand
-constexpr int BM = 128, BN = 128, BK = 32;
+constexpr int S = 6;               // slices per operand
+constexpr int BM = 128, BK = 32;
 constexpr int STAGES = 2;
-constexpr int TILE = BM * BK * 2;                  // one BF16 slice tile, 8 KB (BN == BM)
-constexpr int STAGE_BYTES = 2 * S * TILE;          // 96 KB
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*barriers*/ + 1024 /*alignment*/;
-constexpr int TMEM_COLS = 512;                     // 4 accumulators x BN columns
-constexpr int KMAX = 3072;                         // exactness bound of the CTA's K range
-constexpr int KB_PER_CTA = KMAX / BK;              // 96
+constexpr int KMAX = 3072;         // exactness bound of the K range of one CTA
+constexpr int KB_PER_CTA = KMAX / BK;
 
-static_assert(BN == BM, "one tile size for both operands");
-static_assert(4 * BN <= TMEM_COLS, "four accumulators");
+template <int BN>
+struct Cfg {
+  static constexpr int A_TILE = BM * BK * 2;                 // 8 KB
+  static constexpr int B_TILE = BN * BK * 2;                 // 8 / 4 KB
+  static constexpr int STAGE_BYTES = S * (A_TILE + B_TILE);
+  static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*barriers*/ + 1024 /*alignment*/;
+  static constexpr uint32_t TMEM_COLS = 4 * BN;              // 4 accumulators
+  static_assert(BN == 64 || BN == 128, "tile width");
+};
 
 struct OzArgs {
-  double* out;
-  int64_t ld_out;          // out[mu + ld_out * n]
+  void* out;
   int M, N;
-  int nkb;                 // K blocks of 32 per aux function
-  int total_kb;            // np * nkb
-  int pA0;                 // global aux index of the chunk's first function
-  int depthA, depthB;      // aux functions per slice plane of A (naux) and B (np)
   int m_tiles;
-  const double* rowscale;  // [M] 2^eA
-  const double* colscale;  // [N] alpha * 2^eT
+  int nkb;                  // K blocks of 32 per aux function
+  int total_kb;             // split mode: K blocks of the chunk (np * nkb)
+  int a_depth, b_depth;     // plane stride of A / B in depth units (slice t at depth t * stride)
+  int a_off, b_off;         // depth offset of the chunk's aux function 0
+  int a_per_p;              // A depth advances with the aux function
+  // split mode epilogue: out (double) [m + ld_out n] += (hi + lo) rowscale[m] colscale[n]
+  const double* rowscale;
+  const double* colscale;
+  int64_t ld_out;
+  // batched mode epilogue: out (float2) [(m % m_div) s_m1 + (m / m_div) s_m2 + n s_n + Pl s_p]
+  //   = 2^(e_row[m] + e_col[(b_off + Pl) N + n]) (hi, lo)
+  const int* e_row;
+  const int* e_col;
+  int64_t m_div, s_m1, s_m2, s_n, s_p;
   int* err;
 };
 
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// (hi, lo) ~ a0 + a1 + a2 + a3 (a0, a1, a2 exact integer sums, a3 rounded)
+__device__ __forceinline__ void combine4(float a0, float a1, float a2, float a3, float& hi, float& lo) {
+  float s, e, e2;
+  two_sum(a0, a1, s, e);
+  two_sum(s, a2, s, e2);
+  e += e2;
+  two_sum(s, a3, s, e2);
+  e += e2;
+  hi = s + e;
+  lo = e - (hi - s);
+}
+
+template <int BN, bool BATCHED>
 __global__ void __launch_bounds__(128, 1)
-    tc_ozaki_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB, OzArgs args) {
+    tc_exact_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB, OzArgs args) {
+  using C = Cfg<BN>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * C::STAGE_BYTES);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 8);
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES), accum = smem_u32(bars + 2 * STAGES);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m_tile = blockIdx.x % args.m_tiles, n_tile = blockIdx.x / args.m_tiles;
+  // split mode: x = tile (M fastest), y = K range; batched mode: x = aux function (CTAs that
+  // share an A tile run together), y = tile
+  const int tile = BATCHED ? (int)blockIdx.y : (int)blockIdx.x;
+  const int m_tile = tile % args.m_tiles, n_tile = tile / args.m_tiles;
   const int m0 = m_tile * BM, n0 = n_tile * BN;
-  const int kb0 = blockIdx.y * KB_PER_CTA;
-  const int total = min(args.total_kb - kb0, KB_PER_CTA);
+  const int kb0 = BATCHED ? 0 : blockIdx.y * KB_PER_CTA;
+  const int total = BATCHED ? args.nkb : min(args.total_kb - kb0, KB_PER_CTA);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -93,7 +131,7 @@ __global__ void __launch_bounds__(128, 1)
     mbar_init(accum, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 2) tmem_alloc(smem_u32(tmem_slot), TMEM_COLS);
+  if (warp == 2) tmem_alloc(smem_u32(tmem_slot), C::TMEM_COLS);
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
@@ -109,20 +147,21 @@ __global__ void __launch_bounds__(128, 1)
         if (!mbar_wait(empty0 + 8 * s, ph ^ 1, args.err)) break;
         issued = it + 1;
         const uint32_t full = full0 + 8 * s;
-        mbar_expect_tx(full, STAGE_BYTES);
+        mbar_expect_tx(full, C::STAGE_BYTES);
         const int kb = kb0 + it;
-        const int P = kb / args.nkb;
-        const int k0 = (kb % args.nkb) * BK;
-        const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+        const int P = BATCHED ? (int)blockIdx.x : kb / args.nkb;
+        const int k0 = (BATCHED ? kb : kb % args.nkb) * BK;
+        const int da = args.a_off + (args.a_per_p ? P : 0);
+        const int db = args.b_off + P;
+        const uint32_t st = smem_u32(smem + s * C::STAGE_BYTES);
 #pragma unroll
         for (int t = 0; t < S; ++t) {
-          tma_load_3d(st + t * TILE, &mA, full, k0, m0, t * args.depthA + args.pA0 + P);
-          tma_load_3d(st + (S + t) * TILE, &mB, full, k0, n0, t * args.depthB + P);
+          tma_load_3d(st + t * C::A_TILE, &mA, full, k0, m0, t * args.a_depth + da);
+          tma_load_3d(st + S * C::A_TILE + t * C::B_TILE, &mB, full, k0, n0, t * args.b_depth + db);
         }
       }
-      for (int it = max(0, issued - STAGES); it < issued; ++it) {
+      for (int it = max(0, issued - STAGES); it < issued; ++it)
         mbar_wait(full0 + 8 * (it % STAGES), (it / STAGES) & 1, nullptr);
-      }
     } else if (warp == 1 && lane == 0) {
       // MMA issuer
       constexpr uint32_t idesc = instr_desc_f16(BM, BN, true);
@@ -131,7 +170,7 @@ __global__ void __launch_bounds__(128, 1)
         const uint32_t ph = (it / STAGES) & 1;
         if (!mbar_wait(full0 + 8 * s, ph, args.err)) break;
         fence_after_sync();
-        const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+        const uint32_t st = smem_u32(smem + s * C::STAGE_BYTES);
 #pragma unroll
         for (int k = 0; k < BK / 16; ++k) {
           const uint64_t dk = (uint64_t)((k * 32) >> 4);  // 16 BF16 = 32 B along K inside the swizzle row
@@ -142,8 +181,8 @@ __global__ void __launch_bounds__(128, 1)
               const int u = g - t;
               const int acc = g < 3 ? g : 3;
               const bool first = it == 0 && k == 0 && t == 0 && g <= 3;
-              mma_f16(tmem + (uint32_t)(acc * BN), smem_desc<64>(st + t * TILE) + dk,
-                      smem_desc<64>(st + (S + u) * TILE) + dk, idesc, first ? 0u : 1u);
+              mma_f16(tmem + (uint32_t)(acc * BN), smem_desc<64>(st + t * C::A_TILE) + dk,
+                      smem_desc<64>(st + S * C::A_TILE + u * C::B_TILE) + dk, idesc, first ? 0u : 1u);
             }
           }
         }
@@ -156,21 +195,41 @@ __global__ void __launch_bounds__(128, 1)
     fence_after_sync();
     if (have && *(volatile int*)args.err == 0) {
       const int row = m0 + warp * 32 + lane;
-      const double rs = row < args.M ? args.rowscale[row] : 0.0;
+      const bool row_ok = row < args.M;
       const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+      double rs = 0.0;
+      int erow = 0;
+      int64_t base = 0;
+      const int Pl = BATCHED ? (int)blockIdx.x : 0;
+      if (row_ok) {
+        if (BATCHED) {
+          erow = args.e_row[row];
+          base = args.m_div > 0 ? (row % args.m_div) * args.s_m1 + (row / args.m_div) * args.s_m2 : row * args.s_m1;
+          base += (int64_t)Pl * args.s_p;
+        } else {
+          rs = args.rowscale[row];
+        }
+      }
       for (int c = 0; c < BN / 32; ++c) {
         float v0[32], v1[32], v2[32], v3[32];
         tmem_ld32(lane_base + (uint32_t)(0 * BN + c * 32), v0);
         tmem_ld32(lane_base + (uint32_t)(1 * BN + c * 32), v1);
         tmem_ld32(lane_base + (uint32_t)(2 * BN + c * 32), v2);
         tmem_ld32(lane_base + (uint32_t)(3 * BN + c * 32), v3);
-        if (row < args.M) {
+        if (row_ok) {
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             const int n = n0 + c * 32 + j;
             if (n < args.N) {
-              const double v = ((double)v0[j] + (double)v1[j]) + ((double)v2[j] + (double)v3[j]);
-              atomicAdd(args.out + row + args.ld_out * (int64_t)n, v * rs * args.colscale[n]);
+              float hi, lo;
+              combine4(v0[j], v1[j], v2[j], v3[j], hi, lo);
+              if (BATCHED) {
+                const int e = erow + args.e_col[(int64_t)(args.b_off + Pl) * args.N + n];
+                reinterpret_cast<float2*>(args.out)[base + n * args.s_n] = make_float2(ldexpf(hi, e), ldexpf(lo, e));
+              } else {
+                const double v = ((double)hi + (double)lo) * (rs * args.colscale[n]);
+                atomicAdd(reinterpret_cast<double*>(args.out) + row + args.ld_out * (int64_t)n, v);
+              }
             }
           }
         }
@@ -180,33 +239,46 @@ __global__ void __launch_bounds__(128, 1)
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
-  if (warp == 2) tmem_dealloc(tmem, TMEM_COLS);
+  if (warp == 2) tmem_dealloc(tmem, C::TMEM_COLS);
 }
 
-// ---- slicing (integer arithmetic on the FP64 bit pattern; the FP64 pipe is not used) ------
-// |x| as an ordered integer key (non-negative doubles order like their bit patterns)
+// ---- slicing (integer arithmetic on the bit patterns; the FP64 pipe is not used) ----------
+// |x| as an ordered integer key (non-negative floats order like their bit patterns)
 __device__ __forceinline__ unsigned long long abs_key(double x) {
   return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
 }
+__device__ __forceinline__ unsigned long long abs_key(float2 x) {
+  return (unsigned long long)(__float_as_uint(x.x) & 0x7FFFFFFFu);
+}
 
-// F = round(x 2^(36 - e)) for |x| < 2^e, so |F| <= 2^36; then the six digits
-// q_0 = round(F / 2^30), q_t = round(R_t / 2^(30 - 6t)) of the running remainder, written
-// as BF16 slices q_t 2^(-6(t+1)) (plane stride `plane`).
-__device__ __forceinline__ void slice6(double x, int e, __nv_bfloat16* dst, int64_t plane) {
+// round(x 2^k) for |x| 2^k <= 2^36, from the FP64 bit pattern
+__device__ __forceinline__ long long fix_round(double x, int k, bool& bad) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
   const int E = (int)((bits >> 52) & 0x7FF);
-  const long long mant = (long long)(bits & 0xFFFFFFFFFFFFFull);
+  if (E == 0x7FF) { bad = true; return 0; }
+  const long long M = E ? (long long)((bits & 0xFFFFFFFFFFFFFull) | (1ull << 52)) : (long long)(bits & 0xFFFFFFFFFFFFFull);
+  const int sh = 1075 - k - (E ? E : 1);  // x = M 2^(E - 1075)
   long long F = 0;
-  if (E != 0x7FF) {
-    const long long M = E ? (mant | (1ll << 52)) : mant;
-    const int sh = 1039 + e - (E ? E : 1);  // x = M 2^(E - 1075), F = M 2^-sh (sh >= 17 for |x| < 2^e)
-    if (sh <= 0) {
-      F = 1ll << 40;                        // |x| >= 2^e cannot happen for a finite max; flag by overflow
-    } else if (sh < 63) {
-      F = (M + (1ll << (sh - 1))) >> sh;
-    }
-    if (bits >> 63) F = -F;
-  }
+  if (sh <= 0) F = M << min(-sh, 10);
+  else if (sh < 63) F = (M + (1ll << (sh - 1))) >> sh;
+  return (bits >> 63) ? -F : F;
+}
+// same from the FP32 bit pattern
+__device__ __forceinline__ long long fix_round(float x, int k, bool& bad) {
+  const unsigned bits = __float_as_uint(x);
+  const int E = (int)((bits >> 23) & 0xFF);
+  if (E == 0xFF) { bad = true; return 0; }
+  const long long M = E ? (long long)((bits & 0x7FFFFFu) | 0x800000u) : (long long)(bits & 0x7FFFFFu);
+  const int sh = 150 - k - (E ? E : 1);   // x = M 2^(E - 150)
+  long long F = 0;
+  if (sh <= 0) F = M << min(-sh, 40);
+  else if (sh < 63) F = (M + (1ll << (sh - 1))) >> sh;
+  return (bits >> 31) ? -F : F;
+}
+
+// F = round(v 2^36), |F| <= 2^36, into the six digits q_t = round(R_t / 2^(30 - 6t)) of the
+// running remainder, written as BF16 slices q_t 2^(-6(t+1)) (plane stride `plane`).
+__device__ __forceinline__ void digits6(long long F, bool bad, __nv_bfloat16* dst, int64_t plane) {
   long long R = F;
 #pragma unroll
   for (int t = 0; t < S; ++t) {
@@ -214,39 +286,80 @@ __device__ __forceinline__ void slice6(double x, int e, __nv_bfloat16* dst, int6
     const long long q = s > 0 ? ((R + (1ll << (s - 1))) >> s) : R;
     R -= q << s;
     float v = (float)(int)q * __int_as_float((127 - 6 * (t + 1)) << 23);  // q 2^(-6(t+1)), exact
-    if (E == 0x7FF) v = __int_as_float(0x7FC00000);                        // NaN / Inf propagate as NaN
+    if (bad) v = __int_as_float(0x7FC00000);                                // NaN / Inf propagate as NaN
     dst[t * plane] = __float2bfloat16_rn(v);
   }
 }
+__device__ __forceinline__ void slice6(double x, int e, __nv_bfloat16* dst, int64_t plane) {
+  bool bad = false;
+  const long long F = fix_round(x, 36 - e, bad);
+  digits6(F, bad, dst, plane);
+}
+__device__ __forceinline__ void slice6(float2 x, int e, __nv_bfloat16* dst, int64_t plane) {
+  bool bad = false;
+  const long long F = fix_round(x.x, 36 - e, bad) + fix_round(x.y, 36 - e, bad);
+  digits6(F, bad, dst, plane);
+}
 
 // power of two strictly above max |x| (exponent e with max = f 2^e, f in [0.5, 1)); 0 for zero
-__device__ __forceinline__ int pow2_exp(double m) {
-  if (!(m > 0.0) || !isfinite(m)) return 0;
+__device__ __forceinline__ int key_exp(unsigned long long key, bool is_float) {
+  if (is_float) {
+    const int E = (int)((key >> 23) & 0xFF);
+    if (key == 0 || E == 0xFF) return 0;
+    int e;
+    frexpf(__uint_as_float((unsigned)key), &e);
+    return e;
+  }
+  const int E = (int)((key >> 52) & 0x7FF);
+  if (key == 0 || E == 0x7FF) return 0;
   int e;
-  frexp(m, &e);
+  frexp(__longlong_as_double((long long)key), &e);
   return e;
 }
 
-// max |B_P[mu, nu]| over (nu, P) per row mu; Bd [P][nu][mu] (mu fastest)
-__global__ void rowmax_cderi_kernel(const double* __restrict__ Bd, int64_t nao, int64_t nrows_total,
-                                    unsigned long long* __restrict__ mx) {
+// Generic row slicer: row r, element k at src[(r % rdiv) rs1 + (r / rdiv) rs2 + k ks]
+// (rdiv = 0: r rs1 + k ks); one warp per row: exponent of the row max, then the six slices
+// to dst[t plane + r ld + k]; e_out[r] = exponent, scale_out[r] = 2^exponent (if non-null).
+__global__ void slice_rows_kernel(const double* __restrict__ src, int64_t rows, int64_t K, int64_t rdiv, int64_t rs1,
+                                  int64_t rs2, int64_t ks, __nv_bfloat16* __restrict__ dst, int64_t ld, int64_t plane,
+                                  int* __restrict__ e_out, double* __restrict__ scale_out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t r = w0; r < rows; r += nw) {
+    const double* p = src + (rdiv > 0 ? (r % rdiv) * rs1 + (r / rdiv) * rs2 : r * rs1);
+    unsigned long long m = 0;
+    for (int64_t k = lane; k < K; k += 32) m = max(m, abs_key(p[k * ks]));
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    const int e = key_exp(m, false);
+    for (int64_t k = lane; k < K; k += 32) slice6(p[k * ks], e, dst + r * ld + k, plane);
+    if (lane == 0) {
+      e_out[r] = e;
+      if (scale_out) scale_out[r] = ldexp(1.0, e);
+    }
+  }
+}
+
+// max |X[mu + n r]| over r in [0, nr) per mu (X col-major [n, nr]); atomics per thread
+__global__ void rowmax_strided_kernel(const double* __restrict__ X, int64_t n, int64_t nr,
+                                      unsigned long long* __restrict__ mx) {
   const int64_t mu = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (mu >= nao) return;
+  if (mu >= n) return;
   unsigned long long m = 0;
-  for (int64_t r = blockIdx.y; r < nrows_total; r += gridDim.y) m = max(m, abs_key(Bd[mu + nao * r]));
+  for (int64_t r = blockIdx.y; r < nr; r += gridDim.y) m = max(m, abs_key(X[mu + n * r]));
   atomicMax(mx + mu, m);
 }
 
-__global__ void exp_scale_kernel(const unsigned long long* __restrict__ mx, int64_t n, double mult,
+__global__ void exp_scale_kernel(const unsigned long long* __restrict__ mx, int64_t n, double mult, bool is_float,
                                  int* __restrict__ e_out, double* __restrict__ scale) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int e = pow2_exp(__longlong_as_double((long long)mx[i]));
+  const int e = key_exp(mx[i], is_float);
   e_out[i] = e;
   scale[i] = mult * ldexp(1.0, e);
 }
 
-// A slices [t][P][mu][ldk] of v = B_P[mu, nu] 2^-e_mu (B_P symmetric: read Bd[nu + nao mu + nao^2 P])
+// cderi slices [t][P][mu][ldk] of B_P[mu, nu] 2^-e_mu (B_P symmetric: read Bd[nu + nao mu + nao^2 P])
 __global__ void slice_cderi_kernel(const double* __restrict__ Bd, int64_t nao, int64_t naux, int64_t ldk,
                                    const int* __restrict__ e_row, __nv_bfloat16* __restrict__ out) {
   const int64_t total = naux * nao * nao;
@@ -254,38 +367,53 @@ __global__ void slice_cderi_kernel(const double* __restrict__ Bd, int64_t nao, i
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t nu = t % nao;
     const int64_t r = t / nao;  // P * nao + mu
-    const int64_t mu = r % nao;
-    slice6(Bd[t], e_row[mu], out + nu + ldk * r, plane);
+    slice6(Bd[t], e_row[r % nao], out + nu + ldk * r, plane);
   }
 }
 
-// max |T[Pl][n][nu]| over (Pl, nu < nao) per column n: one warp per row (Pl, n)
-__global__ void colmax_t_kernel(const double* __restrict__ T, int64_t rows, int64_t N, int64_t ldk, int64_t nao,
-                                unsigned long long* __restrict__ mx) {
+// Z^T slices [t][P][mu][ldj] of Z_P[mu, j] 2^-e_mu, Z col-major [nao, nocc, naux]
+__global__ void slice_zt_kernel(const double* __restrict__ Z, int64_t nao, int64_t no, int64_t naux, int64_t ldj,
+                                const int* __restrict__ e_row, __nv_bfloat16* __restrict__ out) {
+  const int64_t total = nao * no * naux;
+  const int64_t plane = naux * nao * ldj;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t mu = t % nao;
+    const int64_t r = t / nao;  // j + no * P
+    const int64_t j = r % no, P = r / no;
+    slice6(Z[t], e_row[mu], out + j + ldj * (mu + nao * P), plane);
+  }
+}
+
+// max |hi| of FP32-pair staging rows (Pl, n) of length K (row stride ld) per column n: one warp per row
+__global__ void colmax_pair_kernel(const float2* __restrict__ T, int64_t rows, int64_t N, int64_t ld, int64_t K,
+                                   unsigned long long* __restrict__ mx) {
   const int lane = threadIdx.x & 31;
   const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t r = w0; r < rows; r += nw) {
     unsigned long long m = 0;
-    for (int64_t k = lane; k < nao; k += 32) m = max(m, abs_key(T[r * ldk + k]));
+    for (int64_t k = lane; k < K; k += 32) m = max(m, abs_key(T[r * ld + k]));
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
     if (lane == 0) atomicMax(mx + (r % N), m);
   }
 }
 
-// B slices [u][Pl][n][ldk] of v = T[Pl][n][nu] 2^-e_n
-__global__ void slice_t_kernel(const double* __restrict__ T, int64_t rows, int64_t N, int64_t ldk, int64_t nao,
-                               const int* __restrict__ e_col, __nv_bfloat16* __restrict__ out) {
-  const int64_t total = rows * nao;
-  const int64_t plane = rows * ldk;
+// slices [t][Pl][n][ld] of the FP32-pair staging T[Pl][n][k] 2^-e_n, k < K
+__global__ void slice_pair_kernel(const float2* __restrict__ T, int64_t rows, int64_t N, int64_t ld, int64_t K,
+                                  const int* __restrict__ e_col, __nv_bfloat16* __restrict__ out) {
+  const int64_t total = rows * K;
+  const int64_t plane = rows * ld;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t k = t % nao;
-    const int64_t r = t / nao;
-    slice6(T[r * ldk + k], e_col[r % N], out + r * ldk + k, plane);
+    const int64_t k = t % K;
+    const int64_t r = t / K;
+    slice6(T[r * ld + k], e_col[r % N], out + r * ld + k, plane);
   }
 }
 
 unsigned grid_for(int64_t total) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(div_up(total, 256), 1 << 20)); }
+unsigned grid_warps(int64_t rows, int num_sms) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(div_up(rows * 32, 256), 16 * (int64_t)num_sms));
+}
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -303,15 +431,15 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 3-D BF16 tensor map: dims {K, rows, depth}, row stride ldk elements, box {32, 128, 1}, 64B swizzle.
-CUtensorMap make_map(const void* base, int64_t K, int64_t rows, int64_t depth, int64_t ldk) {
+// 3-D BF16 tensor map: dims {K, rows, depth}, row stride ld elements, box {32, box_rows, 1}, 64B swizzle.
+CUtensorMap make_map(const void* base, int64_t K, int64_t rows, int64_t depth, int64_t ld, int box_rows) {
   CUtensorMap m;
   std::memset(&m, 0, sizeof(m));
   auto fn = encode_fn();
   if (!fn) throw Error(CPHF_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
   cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)depth};
-  cuuint64_t strides[2] = {(cuuint64_t)(ldk * 2), (cuuint64_t)(ldk * 2 * rows)};
-  cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)BM, 1};
+  cuuint64_t strides[2] = {(cuuint64_t)(ld * 2), (cuuint64_t)(ld * 2 * rows)};
+  cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = fn(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -320,22 +448,53 @@ CUtensorMap make_map(const void* base, int64_t K, int64_t rows, int64_t depth, i
   return m;
 }
 
+template <int BN, bool BATCHED>
+bool set_smem_attr() {
+  return cudaFuncSetAttribute(tc_exact_kernel<BN, BATCHED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              Cfg<BN>::SMEM_BYTES) == cudaSuccess;
+}
+
+// split mode: grid (tiles, K ranges = count); batched mode: grid (aux functions = count, tiles)
+template <int BN, bool BATCHED>
+void launch_exact(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, const OzArgs& a, unsigned count) {
+  const unsigned tiles = (unsigned)(a.m_tiles * div_up(a.N, BN));
+  if (tiles > (BATCHED ? 65535u : 0x7FFFFFFFu) || count > (BATCHED ? 0x7FFFFFFFu : 65535u))
+    throw Error(CPHF_ERR_ARG, "tensor-core K term: grid too large");
+  const dim3 grid = BATCHED ? dim3(count, tiles) : dim3(tiles, count);
+  tc_exact_kernel<BN, BATCHED><<<grid, 128, Cfg<BN>::SMEM_BYTES, c->stream>>>(mA, mB, a);
+  count_launch();
+  CPHF_CUDA(cudaGetLastError());
+}
+
+OzArgs base_args(OzState& z, int M, int N) {
+  OzArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.M = M;
+  a.N = N;
+  a.m_tiles = (int)div_up(M, BM);
+  a.err = z.err.as<int>();
+  return a;
+}
+
 }  // namespace
 
 bool oz_available(cphf_ctx* c) {
   int major = 0;
   cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, c->device);
   if (major != 10 || encode_fn() == nullptr) return false;
-  static bool attr_set = false;
-  if (!attr_set) {
-    if (cudaFuncSetAttribute(tc_ozaki_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) !=
-        cudaSuccess) {
-      cudaGetLastError();
-      return false;
-    }
-    attr_set = true;
+  static bool attr_ok = false, tried = false;
+  if (!tried) {
+    tried = true;
+    attr_ok = set_smem_attr<128, false>() && set_smem_attr<64, true>() && set_smem_attr<128, true>();
+    if (!attr_ok) cudaGetLastError();
   }
-  return true;
+  return attr_ok;
+}
+
+bool oz_supported(const cphf_ctx* c) {
+  for (int s = 0; s < c->nspin; ++s)
+    if (c->spin[s].nocc > KMAX) return false;
+  return c->nao <= KMAX;
 }
 
 void oz_prepare_cderi(cphf_ctx* c, OzState& z) {
@@ -345,79 +504,181 @@ void oz_prepare_cderi(cphf_ctx* c, OzState& z) {
   z.rowscale.ensure((size_t)nao * 8, c->counter());
   z.e_row.ensure((size_t)nao * 4, c->counter());
   z.mx.ensure((size_t)std::max<int64_t>(nao, 1) * 8, c->counter());
+  z.err.ensure(sizeof(int), c->counter());
   CPHF_CUDA(cudaMemsetAsync(z.mx.p, 0, (size_t)nao * 8, c->stream));
   const unsigned gx = (unsigned)div_up(nao, 256);
   const unsigned gy = (unsigned)std::max<int64_t>(1, std::min<int64_t>(nao * naux, 8 * (int64_t)c->num_sms / gx + 1));
-  rowmax_cderi_kernel<<<dim3(gx, gy), 256, 0, c->stream>>>(c->Bd.as<double>(), nao, nao * naux,
-                                                            z.mx.as<unsigned long long>());
-  exp_scale_kernel<<<grid_for(nao), 256, 0, c->stream>>>(z.mx.as<unsigned long long>(), nao, 1.0, z.e_row.as<int>(),
-                                                         z.rowscale.as<double>());
+  rowmax_strided_kernel<<<dim3(gx, gy), 256, 0, c->stream>>>(c->Bd.as<double>(), nao, nao * naux,
+                                                              z.mx.as<unsigned long long>());
+  exp_scale_kernel<<<grid_for(nao), 256, 0, c->stream>>>(z.mx.as<unsigned long long>(), nao, 1.0, false,
+                                                         z.e_row.as<int>(), z.rowscale.as<double>());
   slice_cderi_kernel<<<grid_for(naux * nao * nao), 256, 0, c->stream>>>(c->Bd.as<double>(), nao, naux, z.ldk,
                                                                         z.e_row.as<int>(), z.A.as<__nv_bfloat16>());
   count_launch(3);
   CPHF_CUDA(cudaGetLastError());
+  for (auto& sp : z.spin) sp.ready = false;
   z.ready = true;
 }
 
-void oz_k_term1(cphf_ctx* c, OzState& z, const double* bra, const double* O64, int64_t no, int64_t nb,
-                double alpha, double* out) {
-  if (!z.ready) oz_prepare_cderi(c, z);
-  const int64_t nao = c->nao, naux = c->naux, ldk = z.ldk;
+// O, Z (K = nu) and Z^T (K = j) slices of one spin
+static void oz_prepare_spin(cphf_ctx* c, OzState& z, int s) {
+  const SpinState& sp = c->spin[s];
+  OzSpin& o = z.spin[s];
+  const int64_t nao = c->nao, naux = c->naux, no = sp.nocc, ldk = z.ldk;
+  const int64_t ldj = o.ldj = (no + 7) / 8 * 8;
+  // O_P[j, i]: rows (i, P) at O + no (i + no P), K = j
+  o.O.ensure((size_t)S * naux * no * ldj * 2, c->counter());
+  o.eO.ensure((size_t)naux * no * 4, c->counter());
+  slice_rows_kernel<<<grid_warps(naux * no, c->num_sms), 256, 0, c->stream>>>(
+      sp.O.as<double>(), naux * no, no, 0, no, 0, 1, o.O.as<__nv_bfloat16>(), ldj, naux * no * ldj, o.eO.as<int>(),
+      nullptr);
+  // Z_P[nu, i]: rows (i, P) at Z + nao (i + no P), K = nu
+  o.Z.ensure((size_t)S * naux * no * ldk * 2, c->counter());
+  o.eZ.ensure((size_t)naux * no * 4, c->counter());
+  slice_rows_kernel<<<grid_warps(naux * no, c->num_sms), 256, 0, c->stream>>>(
+      sp.Z.as<double>(), naux * no, nao, 0, nao, 0, 1, o.Z.as<__nv_bfloat16>(), ldk, naux * no * ldk, o.eZ.as<int>(),
+      nullptr);
+  // Z_P[mu, j]: rows mu (scale over all j, P), per-P blocks of K = j
+  o.Zt.ensure((size_t)S * naux * nao * ldj * 2, c->counter());
+  o.sZt.ensure((size_t)nao * 8, c->counter());
+  o.eZt.ensure((size_t)nao * 4, c->counter());
+  CPHF_CUDA(cudaMemsetAsync(z.mx.p, 0, (size_t)nao * 8, c->stream));
+  const unsigned gx = (unsigned)div_up(nao, 256);
+  const unsigned gy = (unsigned)std::max<int64_t>(1, std::min<int64_t>(no * naux, 8 * (int64_t)c->num_sms / gx + 1));
+  rowmax_strided_kernel<<<dim3(gx, gy), 256, 0, c->stream>>>(sp.Z.as<double>(), nao, no * naux,
+                                                              z.mx.as<unsigned long long>());
+  exp_scale_kernel<<<grid_for(nao), 256, 0, c->stream>>>(z.mx.as<unsigned long long>(), nao, 1.0, false,
+                                                         o.eZt.as<int>(), o.sZt.as<double>());
+  slice_zt_kernel<<<grid_for(nao * no * naux), 256, 0, c->stream>>>(sp.Z.as<double>(), nao, no, naux, ldj,
+                                                                    o.eZt.as<int>(), o.Zt.as<__nv_bfloat16>());
+  count_launch(5);
+  CPHF_CUDA(cudaGetLastError());
+  o.ready = true;
+}
+
+void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, double alpha, double* out) {
+  const int64_t nao = c->nao, naux = c->naux, no = c->spin[s].nocc;
   const int64_t N = no * nb;
   if (N <= 0 || nao <= 0) return;
-  // chunk of aux functions: FP64 T staging (8 B) + 6 BF16 slices (12 B) per element within ~3 GiB
-  int64_t np = std::max<int64_t>(1, (int64_t(3) << 30) / std::max<int64_t>(20 * N * ldk, 1));
+  if (!z.ready) oz_prepare_cderi(c, z);
+  OzSpin& os = z.spin[s];
+  if (!os.ready) oz_prepare_spin(c, z, s);
+  const int64_t ldk = z.ldk, ldj = os.ldj;
+  CPHF_CUDA(cudaMemsetAsync(z.err.p, 0, sizeof(int), c->stream));
+
+  // bra slices, both K orders: rows (j, a) over nu (W-gen A) and rows (nu, a) over j (T-gen A)
+  z.braw.ensure((size_t)S * N * ldk * 2, c->counter());
+  z.ebraw.ensure((size_t)N * 4, c->counter());
+  slice_rows_kernel<<<grid_warps(N, c->num_sms), 256, 0, c->stream>>>(
+      bra, N, nao, 0, nao, 0, 1, z.braw.as<__nv_bfloat16>(), ldk, N * ldk, z.ebraw.as<int>(), nullptr);
+  z.brat.ensure((size_t)S * nao * nb * ldj * 2, c->counter());
+  z.ebrat.ensure((size_t)nao * nb * 4, c->counter());
+  slice_rows_kernel<<<grid_warps(nao * nb, c->num_sms), 256, 0, c->stream>>>(
+      bra, nao * nb, no, nao, 1, nao * no, nao, z.brat.as<__nv_bfloat16>(), ldj, nao * nb * ldj, z.ebrat.as<int>(),
+      nullptr);
+  count_launch(2);
+
+  // chunk of aux functions: T staging (FP32 pair, 8 B) + slices (12 B) per element within ~8 GiB
+  int64_t np = std::max<int64_t>(1, (int64_t(8) << 30) / std::max<int64_t>(20 * N * ldk, 1));
   if (c->cfg.aux_chunk > 0) np = c->cfg.aux_chunk;
-  np = std::min<int64_t>(np, naux);
+  np = std::min<int64_t>(std::min<int64_t>(np, naux), 65535);
   z.T.ensure((size_t)np * N * ldk * 8, c->counter());
   z.B.ensure((size_t)S * np * N * ldk * 2, c->counter());
+  z.W.ensure((size_t)np * N * ldj * 8, c->counter());
+  z.Ws.ensure((size_t)S * np * N * ldj * 2, c->counter());
   z.colscale.ensure((size_t)N * 8, c->counter());
   z.e_col.ensure((size_t)N * 4, c->counter());
   z.mxc.ensure((size_t)N * 8, c->counter());
-  z.err.ensure(sizeof(int), c->counter());
-  CPHF_CUDA(cudaMemsetAsync(z.err.p, 0, sizeof(int), c->stream));
-  const int m_tiles = (int)div_up(nao, BM), n_tiles = (int)div_up(N, BN);
-  const int nkb = (int)div_up(nao, BK);
-  const CUtensorMap mA = make_map(z.A.p, nao, nao, S * naux, ldk);
+
+  const CUtensorMap mCd = make_map(z.A.p, nao, nao, S * naux, ldk, BM);            // term 1 A
+  const CUtensorMap mBt = make_map(z.brat.p, no, nao * nb, S, ldj, BM);            // T-gen A
+  const CUtensorMap mO = make_map(os.O.p, no, no, S * naux, ldj, 64);               // T-gen B
+  const CUtensorMap mBw = make_map(z.braw.p, nao, N, S, ldk, BM);                  // W-gen A
+  const CUtensorMap mZ = make_map(os.Z.p, nao, no, S * naux, ldk, 64);             // W-gen B
+  const CUtensorMap mZt = make_map(os.Zt.p, no, nao, S * naux, ldj, BM);           // term 2 A
+  const int nkb_nao = (int)div_up(nao, BK), nkb_no = (int)div_up(no, BK);
+
   for (int64_t P0 = 0; P0 < naux; P0 += np) {
     const int64_t npc = std::min<int64_t>(np, naux - P0);
-    // T[Pl][(i,a)][nu] = sum_j bra[nu, j, a] O_P[j, i] in FP64 (rows (nu, a) two-level, columns i)
-    GemmDesc t;
-    t.M = nao * nb; t.N = no; t.K = no; t.batch1 = npc;
-    t.A = bra; t.a_m = 1; t.m_div = nao; t.a_m2 = nao * no; t.a_k = nao; t.a_b1 = 0;
-    t.B = O64 + P0 * no * no; t.b_k = 1; t.b_n = no; t.b_b1 = no * no;
-    t.C = z.T.p; t.c_m = 1; t.c_m2 = ldk * no; t.c_n = ldk; t.c_b1 = N * ldk;
-    gemm64(c, t);
-    CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
     const int64_t rows = npc * N;
-    colmax_t_kernel<<<(unsigned)std::min<int64_t>(div_up(rows * 32, 256), 16 * (int64_t)c->num_sms), 256, 0,
-                      c->stream>>>(z.T.as<double>(), rows, N, ldk, nao, z.mxc.as<unsigned long long>());
-    exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha,
+    {
+      // T-gen: T[Pl][(i,a)][nu] (FP32 pair), rows m = nu + nao a, columns i, K = j
+      OzArgs a = base_args(z, (int)(nao * nb), (int)no);
+      a.out = z.T.p;
+      a.nkb = nkb_no;
+      a.a_depth = 1;
+      a.b_depth = (int)naux;
+      a.b_off = (int)P0;
+      a.e_row = z.ebrat.as<int>();
+      a.e_col = os.eO.as<int>();
+      a.m_div = nao; a.s_m1 = 1; a.s_m2 = ldk * no; a.s_n = ldk; a.s_p = N * ldk;
+      ProfScope ps(c, PROF_TC_OZAKI, 2.0 * nao * nb * no * no * npc, 0.0);
+      launch_exact<64, true>(c, mBt, mO, a, (unsigned)npc);
+    }
+    CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
+    colmax_pair_kernel<<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
+                                                                             z.mxc.as<unsigned long long>());
+    exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true,
                                                          z.e_col.as<int>(), z.colscale.as<double>());
-    slice_t_kernel<<<grid_for(rows * nao), 256, 0, c->stream>>>(z.T.as<double>(), rows, N, ldk, nao,
-                                                                z.e_col.as<int>(), z.B.as<__nv_bfloat16>());
+    slice_pair_kernel<<<grid_for(rows * nao), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
+                                                                   z.e_col.as<int>(), z.B.as<__nv_bfloat16>());
     count_launch(3);
-    const CUtensorMap mB = make_map(z.B.p, nao, N, S * npc, ldk);
-    OzArgs a;
-    a.out = out;
-    a.ld_out = nao;
-    a.M = (int)nao;
-    a.N = (int)N;
-    a.nkb = nkb;
-    a.total_kb = (int)(npc * nkb);
-    a.pA0 = (int)P0;
-    a.depthA = (int)naux;
-    a.depthB = (int)npc;
-    a.m_tiles = m_tiles;
-    a.rowscale = z.rowscale.as<double>();
-    a.colscale = z.colscale.as<double>();
-    a.err = z.err.as<int>();
-    dim3 grid((unsigned)(m_tiles * n_tiles), (unsigned)div_up(npc * nkb, KB_PER_CTA));
-    // algorithmic FLOPs of the FP64 contraction (the tensor pipe executes 21 slice products)
-    ProfScope ps(c, PROF_TC_OZAKI, 2.0 * nao * N * nao * npc, 2.0 * S * nao * npc * (nao + N));
-    tc_ozaki_kernel<<<grid, 128, SMEM_BYTES, c->stream>>>(mA, mB, a);
-    count_launch();
-    CPHF_CUDA(cudaGetLastError());
+    {
+      // term 1: out[mu, n] += alpha sum_{P, nu} B_P[mu, nu] T_P[nu, n]
+      const CUtensorMap mT = make_map(z.B.p, nao, N, S * npc, ldk, BM);
+      OzArgs a = base_args(z, (int)nao, (int)N);
+      a.out = out;
+      a.nkb = nkb_nao;
+      a.total_kb = (int)(npc * nkb_nao);
+      a.a_depth = (int)naux;
+      a.a_off = (int)P0;
+      a.a_per_p = 1;
+      a.b_depth = (int)npc;
+      a.rowscale = z.rowscale.as<double>();
+      a.colscale = z.colscale.as<double>();
+      a.ld_out = nao;
+      ProfScope ps(c, PROF_TC_OZAKI, 2.0 * nao * N * nao * npc, 2.0 * S * nao * npc * (nao + N));
+      launch_exact<128, false>(c, mCd, mT, a, (unsigned)div_up(a.total_kb, KB_PER_CTA));
+    }
+    {
+      // W-gen: W[Pl][(i,a)][j] (FP32 pair), rows m = j + no a, columns i, K = nu
+      OzArgs a = base_args(z, (int)N, (int)no);
+      a.out = z.W.p;
+      a.nkb = nkb_nao;
+      a.a_depth = 1;
+      a.b_depth = (int)naux;
+      a.b_off = (int)P0;
+      a.e_row = z.ebraw.as<int>();
+      a.e_col = os.eZ.as<int>();
+      a.m_div = no; a.s_m1 = 1; a.s_m2 = ldj * no; a.s_n = ldj; a.s_p = N * ldj;
+      ProfScope ps(c, PROF_TC_OZAKI, 2.0 * N * no * nao * npc, 0.0);
+      launch_exact<64, true>(c, mBw, mZ, a, (unsigned)npc);
+    }
+    CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
+    colmax_pair_kernel<<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.W.as<float2>(), rows, N, ldj, no,
+                                                                             z.mxc.as<unsigned long long>());
+    exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true,
+                                                         z.e_col.as<int>(), z.colscale.as<double>());
+    slice_pair_kernel<<<grid_for(rows * no), 256, 0, c->stream>>>(z.W.as<float2>(), rows, N, ldj, no,
+                                                                   z.e_col.as<int>(), z.Ws.as<__nv_bfloat16>());
+    count_launch(3);
+    {
+      // term 2: out[mu, n] += alpha sum_{P, j} Z_P[mu, j] W_P[j, n]
+      const CUtensorMap mW = make_map(z.Ws.p, no, N, S * npc, ldj, BM);
+      OzArgs a = base_args(z, (int)nao, (int)N);
+      a.out = out;
+      a.nkb = nkb_no;
+      a.total_kb = (int)(npc * nkb_no);
+      a.a_depth = (int)naux;
+      a.a_off = (int)P0;
+      a.a_per_p = 1;
+      a.b_depth = (int)npc;
+      a.rowscale = os.sZt.as<double>();
+      a.colscale = z.colscale.as<double>();
+      a.ld_out = nao;
+      ProfScope ps(c, PROF_TC_OZAKI, 2.0 * nao * N * no * npc, 2.0 * S * no * npc * (nao + N));
+      launch_exact<128, false>(c, mZt, mW, a, (unsigned)div_up(a.total_kb, KB_PER_CTA));
+    }
   }
   int flag = 0;
   CPHF_CUDA(cudaMemcpyAsync(&flag, z.err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
