@@ -51,6 +51,7 @@ def parse():
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison solve")
     p.add_argument("--cpu-sample", type=int, default=12, help="RHS columns of the CPU baseline sample")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg (profiling runs)")
     p.add_argument("--no-learned", action="store_true", help="do not use the trained initial guess")
     p.add_argument("--fp64-tol", type=float, default=1e-10, help="Krylov tol of the plain FP64 solve")
     p.add_argument("--fp64-lindep", type=float, default=1e-20,
@@ -341,7 +342,7 @@ def run_gpu(args, world, rank, local):
                 launches=dom["launches"], avg_launch_ms=dom["ms"] / dom["launches"],
                 share_of_step=dom["ms"] * 1e-3 / (t_step * args.steps))
 
-    cpu = cpu_oracle_estimate(s, args.cpu_sample) if rank == 0 and nspin == 1 else None
+    cpu = cpu_oracle_estimate(s, args.cpu_sample) if rank == 0 and nspin == 1 and not args.no_cpu else None
     st = stats[-1]
     line = dict(
         metric=METRIC, value=t_step, unit="s", n_gpus=args.gpus, steps=args.steps, warmup=args.warmup,

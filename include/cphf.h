@@ -68,9 +68,10 @@ typedef struct cphf_config {
   int32_t fp64_every_step;   /* mixed: FP64 residual after every correction, not only the first (default 0) */
   int64_t xc_chunk_points;   /* grid points per XC chunk (default 0 = 8 GiB of intermediates) */
   int32_t residual_dfloat;   /* mixed: arithmetic of the correction residuals.  0 = native FP64;
-                                1 = double-float GEMMs on the FP32 pipes (~1e-14 relative, default);
-                                2 = as 1, with the RI-K term B_P bra O_P on the tensor cores as exact
-                                BF16 slice products (6 x 6 bits, ~1e-10 relative to sum |B||T|).
+                                1 = double-float GEMMs on the FP32 pipes (~1e-14 relative);
+                                2 = as 1, with the whole RI-K term on the tensor cores as exact BF16
+                                slice products (6 x 6 bits, ~1e-10 relative to the operand row maxima;
+                                default; without tensor cores it behaves as 1).
                                 The final verification (verify_residual) is always native FP64. */
 } cphf_config;
 

@@ -149,7 +149,7 @@ cphf_status cphf_config_default(cphf_config* cfg) {
   cfg->verify_residual = 1;
   cfg->fp64_every_step = 0;
   cfg->xc_chunk_points = 0;
-  cfg->residual_dfloat = 1;
+  cfg->residual_dfloat = 2;
   return CPHF_OK;
 }
 

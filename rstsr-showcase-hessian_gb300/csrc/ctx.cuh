@@ -40,6 +40,7 @@ struct LowpState {
   DevBuf Bhi, Blo;             // FP16 hi / lo split of the dense cderi for the tensor-core K term
   int64_t ldk = 0;             // padded row length of the FP16 copies
   OzState oz;                  // FP64-accurate tensor-core K term of the residual
+  OzState lp;                  // split-FP16 planes of O, Z and bra for the K term's other contractions
   DevBuf phi32;
   DevBuf s_c1, s_resp, s_T, s_W, s_d, s_ket, s_rho, s_y, s_x, s_Thi, s_Tlo, s_acc;
   DevBuf err;                  // device error flag of the tensor-core kernels (bounded waits)

@@ -31,7 +31,8 @@ void lowp_prepare(cphf_ctx* c) {
   L.err.ensure(sizeof(int), c->counter());
   CPHF_CUDA(cudaMemsetAsync(L.err.p, 0, sizeof(int), c->stream));
   if (c->has_rijk) {
-    L.use_tc = c->cfg.tensor_cores != 0 && tc_available(c);
+    // tc_available / oz_available also set the kernels' shared-memory limits
+    L.use_tc = c->cfg.tensor_cores != 0 && tc_available(c) && oz_available(c);
     if (L.use_tc) {
       tc_prepare_cderi(c, L.Bhi, L.Blo, L.ldk);
     } else {
@@ -115,15 +116,23 @@ static void rijk_response_lowp(cphf_ctx* c, float* const* bra, int64_t nb, float
       }
       const int64_t np_max = k_chunk_lowp(c, no, nb);
       if (L.use_tc) {
-        // term 1 on the tensor cores: out += -scale_k sum_P B_P (bra O_P)
-        tc_k_term1(c, L.Bhi, L.Blo, L.ldk, sp.O32.as<float>(), bra[s], no, nb, -c->scale_k, out[s],
-                   L.s_Thi, L.s_Tlo);
+        // the whole K term on the tensor cores (split FP16): term 1 with T made by the batched
+        // T-generation kernel, then W-generation and term 2 per chunk
+        int* err = L.err.as<int>();
+        lp_begin(c, L.lp, s, bra[s], nb);
+        tc_k_term1(c, L.Bhi, L.Blo, L.ldk, sp.O32.as<float>(), bra[s], no, nb, -c->scale_k, out[s], L.s_Thi,
+                   L.s_Tlo, [&](int64_t P0, int64_t npc, float* T32) {
+                     lp_tgen(c, L.lp, s, P0, npc, nb, T32, L.ldk, err);
+                   });
+        for (int64_t P0 = 0; P0 < naux; P0 += np_max)
+          lp_w_term2(c, L.lp, s, P0, std::min<int64_t>(np_max, naux - P0), nb, -c->scale_k, out[s], err);
+        continue;
       }
       L.s_T.ensure((size_t)nao * np_max * no * nb * 4, c->counter());
       L.s_W.ensure((size_t)no * np_max * no * nb * 4, c->counter());
       for (int64_t P0 = 0; P0 < naux; P0 += np_max) {
         const int64_t np = std::min<int64_t>(np_max, naux - P0);
-        if (!L.use_tc) {
+        {
           // T[(nu,Pl),(i,a)]: rows (nu, a) two-level, columns i, batch over P
           GemmDesc t;
           t.M = nao * nb; t.N = no; t.K = no; t.batch1 = np;

@@ -315,7 +315,7 @@ void tc_prepare_cderi(cphf_ctx* c, DevBuf& hi, DevBuf& lo, int64_t& ldk) {
 }
 
 void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, const float* O32, const float* bra,
-                int64_t no, int64_t nb, double alpha, float* out, DevBuf& Thi, DevBuf& Tlo) {
+                int64_t no, int64_t nb, double alpha, float* out, DevBuf& Thi, DevBuf& Tlo, const TGen& tgen) {
   LowpState& L = *c->lowp;
   const int64_t nao = c->nao, naux = c->naux;
   const int64_t N = no * nb;
@@ -338,12 +338,16 @@ void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, 
     const int64_t npc = std::min<int64_t>(np, naux - P0);
     // T32[Pl][(i,a)][nu] = sum_j bra[nu, j, a] O_P[j, i]: one tall GEMM per aux function,
     // rows (nu, a) (two-level index), columns i, K = j
-    GemmDesc t;
-    t.M = nao * nb; t.N = no; t.K = no; t.batch1 = npc;
-    t.A = bra; t.a_m = 1; t.m_div = nao; t.a_m2 = nao * no; t.a_k = nao; t.a_b1 = 0;
-    t.B = O32 + P0 * no * no; t.b_k = 1; t.b_n = no; t.b_b1 = no * no;
-    t.C = T32; t.c_m = 1; t.c_m2 = ldk * no; t.c_n = ldk; t.c_b1 = N * ldk;
-    gemm32(c, t);
+    if (tgen) {
+      tgen(P0, npc, T32);
+    } else {
+      GemmDesc t;
+      t.M = nao * nb; t.N = no; t.K = no; t.batch1 = npc;
+      t.A = bra; t.a_m = 1; t.m_div = nao; t.a_m2 = nao * no; t.a_k = nao; t.a_b1 = 0;
+      t.B = O32 + P0 * no * no; t.b_k = 1; t.b_n = no; t.b_b1 = no * no;
+      t.C = T32; t.c_m = 1; t.c_m2 = ldk * no; t.c_n = ldk; t.c_b1 = N * ldk;
+      gemm32(c, t);
+    }
     const int64_t tn = npc * N * ldk;
     CPHF_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned), c->stream));
     absmax_f32_kernel<<<(unsigned)std::min<int64_t>(npc * N, 8 * (int64_t)c->num_sms), 256, 0, c->stream>>>(

@@ -4,6 +4,7 @@
 // products hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory.
 #pragma once
 #include <cstdint>
+#include <functional>
 
 #include "ctx.cuh"
 
@@ -13,9 +14,12 @@ namespace cphf {
 bool tc_available(cphf_ctx* c);
 // FP16 hi/lo copies of the dense cderi, rows of length ldk (K-major for the MMA)
 void tc_prepare_cderi(cphf_ctx* c, DevBuf& hi, DevBuf& lo, int64_t& ldk);
-// out (FP32 [nao, nocc, nb]) += alpha * sum_P B_P bra O_P; bra FP32 [nao, nocc, nb], O32 [nocc, nocc, naux]
+// T generator: T32[Pl][(i,a)][nu] (row stride ldk) = sum_j bra[nu,j,a] O_P[j,i], P in [P0, P0 + npc)
+using TGen = std::function<void(int64_t P0, int64_t npc, float* T32)>;
+// out (FP32 [nao, nocc, nb]) += alpha * sum_P B_P bra O_P; bra FP32 [nao, nocc, nb], O32 [nocc, nocc, naux];
+// T is made by `tgen` when given, else by an FP32 CUDA-core GEMM
 void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, const float* O32,
                 const float* bra, int64_t nocc, int64_t nb, double alpha, float* out, DevBuf& Thi,
-                DevBuf& Tlo);
+                DevBuf& Tlo, const TGen& tgen = TGen());
 
 }  // namespace cphf

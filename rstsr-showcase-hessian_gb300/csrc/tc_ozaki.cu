@@ -33,13 +33,19 @@
 //   warp 2         -- TMEM allocation and release;
 //   warps 0-3      -- epilogue.
 // Every mbarrier wait is bounded; on expiry the kernel raises the error flag and returns.
+//
+// The same kernel template also runs the split-precision operator of the inner solves
+// (Split2): two FP16 planes per operand (x 2^(14-e) = hi + lo), three products hi*hi +
+// hi*lo + lo*hi into one FP32 accumulator, FP32 outputs; ~1e-7 relative to the row maxima.
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 #include "kernels.cuh"
 #include "tc_ozaki.cuh"
@@ -49,20 +55,34 @@ namespace cphf {
 namespace {
 using namespace tcx;
 
-constexpr int S = 6;               // slices per operand
 constexpr int BM = 128, BK = 32;
-constexpr int STAGES = 2;
 constexpr int KMAX = 3072;         // exactness bound of the K range of one CTA
 constexpr int KB_PER_CTA = KMAX / BK;
 
-template <int BN>
+// Operand representations: exact BF16 slices (FP64-accurate residual) and split FP16 hi/lo
+// (the inner solves' operator).  EOFF: exponent offset of the stored planes (x 2^(EOFF - e)).
+struct Exact6 {
+  static constexpr int S = 6, NACC = 4, EOFF = 0, STAGES = 2;
+  static constexpr bool BF16 = true;
+  using Elem = __nv_bfloat16;
+};
+struct Split2 {
+  static constexpr int S = 2, NACC = 1, EOFF = 14, STAGES = 6;
+  static constexpr bool BF16 = false;
+  using Elem = __half;
+};
+constexpr int S = Exact6::S;
+
+template <class PR, int BN>
 struct Cfg {
   static constexpr int A_TILE = BM * BK * 2;                 // 8 KB
   static constexpr int B_TILE = BN * BK * 2;                 // 8 / 4 KB
-  static constexpr int STAGE_BYTES = S * (A_TILE + B_TILE);
+  static constexpr int STAGES = PR::STAGES;
+  static constexpr int STAGE_BYTES = PR::S * (A_TILE + B_TILE);
   static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*barriers*/ + 1024 /*alignment*/;
-  static constexpr uint32_t TMEM_COLS = 4 * BN;              // 4 accumulators
+  static constexpr uint32_t TMEM_COLS = PR::NACC * BN;       // one accumulator per group
   static_assert(BN == 64 || BN == 128, "tile width");
+  static_assert(SMEM_BYTES <= 232448, "shared memory");
 };
 
 struct OzArgs {
@@ -74,12 +94,12 @@ struct OzArgs {
   int a_depth, b_depth;     // plane stride of A / B in depth units (slice t at depth t * stride)
   int a_off, b_off;         // depth offset of the chunk's aux function 0
   int a_per_p;              // A depth advances with the aux function
-  // split mode epilogue: out (double) [m + ld_out n] += (hi + lo) rowscale[m] colscale[n]
+  // split mode epilogue: out [m + ld_out n] += value rowscale[m] colscale[n] (double: Exact6, float: Split2)
   const double* rowscale;
   const double* colscale;
   int64_t ld_out;
-  // batched mode epilogue: out (float2) [(m % m_div) s_m1 + (m / m_div) s_m2 + n s_n + Pl s_p]
-  //   = 2^(e_row[m] + e_col[(b_off + Pl) N + n]) (hi, lo)
+  // batched mode epilogue: out [(m % m_div) s_m1 + (m / m_div) s_m2 + n s_n + Pl s_p]
+  //   = 2^(e_row[m] + e_col[(b_off + Pl) N + n] - 2 EOFF) value (float2 pair: Exact6, float: Split2)
   const int* e_row;
   const int* e_col;
   int64_t m_div, s_m1, s_m2, s_n, s_p;
@@ -104,14 +124,15 @@ __device__ __forceinline__ void combine4(float a0, float a1, float a2, float a3,
   lo = e - (hi - s);
 }
 
-template <int BN, bool BATCHED>
+template <class PR, int BN, bool BATCHED>
 __global__ void __launch_bounds__(128, 1)
-    tc_exact_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB, OzArgs args) {
-  using C = Cfg<BN>;
+    tc_slice_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB, OzArgs args) {
+  using C = Cfg<PR, BN>;
+  constexpr int STAGES = C::STAGES;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * C::STAGE_BYTES);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 8);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES), accum = smem_u32(bars + 2 * STAGES);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -155,35 +176,43 @@ __global__ void __launch_bounds__(128, 1)
         const int db = args.b_off + P;
         const uint32_t st = smem_u32(smem + s * C::STAGE_BYTES);
 #pragma unroll
-        for (int t = 0; t < S; ++t) {
+        for (int t = 0; t < PR::S; ++t) {
           tma_load_3d(st + t * C::A_TILE, &mA, full, k0, m0, t * args.a_depth + da);
-          tma_load_3d(st + S * C::A_TILE + t * C::B_TILE, &mB, full, k0, n0, t * args.b_depth + db);
+          tma_load_3d(st + PR::S * C::A_TILE + t * C::B_TILE, &mB, full, k0, n0, t * args.b_depth + db);
         }
       }
       for (int it = max(0, issued - STAGES); it < issued; ++it)
         mbar_wait(full0 + 8 * (it % STAGES), (it / STAGES) & 1, nullptr);
     } else if (warp == 1 && lane == 0) {
       // MMA issuer
-      constexpr uint32_t idesc = instr_desc_f16(BM, BN, true);
+      constexpr uint32_t idesc = instr_desc_f16(BM, BN, PR::BF16);
       for (int it = 0; it < total; ++it) {
         const int s = it % STAGES;
         const uint32_t ph = (it / STAGES) & 1;
         if (!mbar_wait(full0 + 8 * s, ph, args.err)) break;
         fence_after_sync();
         const uint32_t st = smem_u32(smem + s * C::STAGE_BYTES);
+        const uint32_t sb = st + PR::S * C::A_TILE;
 #pragma unroll
         for (int k = 0; k < BK / 16; ++k) {
-          const uint64_t dk = (uint64_t)((k * 32) >> 4);  // 16 BF16 = 32 B along K inside the swizzle row
+          const uint64_t dk = (uint64_t)((k * 32) >> 4);  // 16 elements = 32 B along K inside the swizzle row
+          if constexpr (PR::NACC == 4) {
 #pragma unroll
-          for (int g = 0; g < S; ++g) {
+            for (int g = 0; g < PR::S; ++g) {
 #pragma unroll
-            for (int t = 0; t <= g; ++t) {
-              const int u = g - t;
-              const int acc = g < 3 ? g : 3;
-              const bool first = it == 0 && k == 0 && t == 0 && g <= 3;
-              mma_f16(tmem + (uint32_t)(acc * BN), smem_desc<64>(st + t * C::A_TILE) + dk,
-                      smem_desc<64>(st + S * C::A_TILE + u * C::B_TILE) + dk, idesc, first ? 0u : 1u);
+              for (int t = 0; t <= g; ++t) {
+                const int u = g - t;
+                const int acc = g < 3 ? g : 3;
+                const bool first = it == 0 && k == 0 && t == 0 && g <= 3;
+                mma_f16(tmem + (uint32_t)(acc * BN), smem_desc<64>(st + t * C::A_TILE) + dk,
+                        smem_desc<64>(sb + u * C::B_TILE) + dk, idesc, first ? 0u : 1u);
+              }
             }
+          } else {
+            // hi*hi + hi*lo + lo*hi
+            mma_f16(tmem, smem_desc<64>(st) + dk, smem_desc<64>(sb) + dk, idesc, (it > 0 || k > 0) ? 1u : 0u);
+            mma_f16(tmem, smem_desc<64>(st) + dk, smem_desc<64>(sb + C::B_TILE) + dk, idesc, 1u);
+            mma_f16(tmem, smem_desc<64>(st + C::A_TILE) + dk, smem_desc<64>(sb) + dk, idesc, 1u);
           }
         }
         mma_commit(empty0 + 8 * s);
@@ -211,24 +240,45 @@ __global__ void __launch_bounds__(128, 1)
         }
       }
       for (int c = 0; c < BN / 32; ++c) {
-        float v0[32], v1[32], v2[32], v3[32];
-        tmem_ld32(lane_base + (uint32_t)(0 * BN + c * 32), v0);
-        tmem_ld32(lane_base + (uint32_t)(1 * BN + c * 32), v1);
-        tmem_ld32(lane_base + (uint32_t)(2 * BN + c * 32), v2);
-        tmem_ld32(lane_base + (uint32_t)(3 * BN + c * 32), v3);
-        if (row_ok) {
+        if constexpr (PR::NACC == 4) {
+          float v0[32], v1[32], v2[32], v3[32];
+          tmem_ld32(lane_base + (uint32_t)(0 * BN + c * 32), v0);
+          tmem_ld32(lane_base + (uint32_t)(1 * BN + c * 32), v1);
+          tmem_ld32(lane_base + (uint32_t)(2 * BN + c * 32), v2);
+          tmem_ld32(lane_base + (uint32_t)(3 * BN + c * 32), v3);
+          if (row_ok) {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int n = n0 + c * 32 + j;
-            if (n < args.N) {
-              float hi, lo;
-              combine4(v0[j], v1[j], v2[j], v3[j], hi, lo);
-              if (BATCHED) {
-                const int e = erow + args.e_col[(int64_t)(args.b_off + Pl) * args.N + n];
-                reinterpret_cast<float2*>(args.out)[base + n * args.s_n] = make_float2(ldexpf(hi, e), ldexpf(lo, e));
-              } else {
-                const double v = ((double)hi + (double)lo) * (rs * args.colscale[n]);
-                atomicAdd(reinterpret_cast<double*>(args.out) + row + args.ld_out * (int64_t)n, v);
+            for (int j = 0; j < 32; ++j) {
+              const int n = n0 + c * 32 + j;
+              if (n < args.N) {
+                float hi, lo;
+                combine4(v0[j], v1[j], v2[j], v3[j], hi, lo);
+                if (BATCHED) {
+                  const int e = erow + args.e_col[(int64_t)(args.b_off + Pl) * args.N + n] - 2 * PR::EOFF;
+                  reinterpret_cast<float2*>(args.out)[base + n * args.s_n] =
+                      make_float2(ldexpf(hi, e), ldexpf(lo, e));
+                } else {
+                  const double v = ((double)hi + (double)lo) * (rs * args.colscale[n]);
+                  atomicAdd(reinterpret_cast<double*>(args.out) + row + args.ld_out * (int64_t)n, v);
+                }
+              }
+            }
+          }
+        } else {
+          float v[32];
+          tmem_ld32(lane_base + (uint32_t)(c * 32), v);
+          if (row_ok) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              const int n = n0 + c * 32 + j;
+              if (n < args.N) {
+                if (BATCHED) {
+                  const int e = erow + args.e_col[(int64_t)(args.b_off + Pl) * args.N + n] - 2 * PR::EOFF;
+                  reinterpret_cast<float*>(args.out)[base + n * args.s_n] = ldexpf(v[j], e);
+                } else {
+                  atomicAdd(reinterpret_cast<float*>(args.out) + row + args.ld_out * (int64_t)n,
+                            v[j] * (float)(rs * args.colscale[n]));
+                }
               }
             }
           }
@@ -250,6 +300,11 @@ __device__ __forceinline__ unsigned long long abs_key(double x) {
 __device__ __forceinline__ unsigned long long abs_key(float2 x) {
   return (unsigned long long)(__float_as_uint(x.x) & 0x7FFFFFFFu);
 }
+__device__ __forceinline__ unsigned long long abs_key(float x) {
+  return (unsigned long long)(__float_as_uint(x) & 0x7FFFFFFFu);
+}
+template <class T>
+__host__ __device__ constexpr bool float_key() { return !std::is_same<T, double>::value; }
 
 // round(x 2^k) for |x| 2^k <= 2^36, from the FP64 bit pattern
 __device__ __forceinline__ long long fix_round(double x, int k, bool& bad) {
@@ -301,6 +356,24 @@ __device__ __forceinline__ void slice6(float2 x, int e, __nv_bfloat16* dst, int6
   digits6(F, bad, dst, plane);
 }
 
+// store one element's planes: exact BF16 slices, or split FP16 hi/lo of x 2^(14 - e)
+template <class PR>
+struct Put;
+template <>
+struct Put<Exact6> {
+  template <class T>
+  __device__ static void put(T x, int e, __nv_bfloat16* dst, int64_t plane) { slice6(x, e, dst, plane); }
+};
+template <>
+struct Put<Split2> {
+  __device__ static void put(float x, int e, __half* dst, int64_t plane) {
+    const float v = ldexpf(x, Split2::EOFF - e);
+    const __half h = __float2half_rn(v);
+    dst[0] = h;
+    dst[plane] = __float2half_rn(v - __half2float(h));
+  }
+};
+
 // power of two strictly above max |x| (exponent e with max = f 2^e, f in [0.5, 1)); 0 for zero
 __device__ __forceinline__ int key_exp(unsigned long long key, bool is_float) {
   if (is_float) {
@@ -320,28 +393,27 @@ __device__ __forceinline__ int key_exp(unsigned long long key, bool is_float) {
 // Generic row slicer: row r, element k at src[(r % rdiv) rs1 + (r / rdiv) rs2 + k ks]
 // (rdiv = 0: r rs1 + k ks); one warp per row: exponent of the row max, then the six slices
 // to dst[t plane + r ld + k]; e_out[r] = exponent, scale_out[r] = 2^exponent (if non-null).
-__global__ void slice_rows_kernel(const double* __restrict__ src, int64_t rows, int64_t K, int64_t rdiv, int64_t rs1,
-                                  int64_t rs2, int64_t ks, __nv_bfloat16* __restrict__ dst, int64_t ld, int64_t plane,
-                                  int* __restrict__ e_out, double* __restrict__ scale_out) {
+template <class PR, class TIn>
+__global__ void slice_rows_kernel(const TIn* __restrict__ src, int64_t rows, int64_t K, int64_t rdiv, int64_t rs1,
+                                  int64_t rs2, int64_t ks, typename PR::Elem* __restrict__ dst, int64_t ld,
+                                  int64_t plane, int* __restrict__ e_out) {
   const int lane = threadIdx.x & 31;
   const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t r = w0; r < rows; r += nw) {
-    const double* p = src + (rdiv > 0 ? (r % rdiv) * rs1 + (r / rdiv) * rs2 : r * rs1);
+    const TIn* p = src + (rdiv > 0 ? (r % rdiv) * rs1 + (r / rdiv) * rs2 : r * rs1);
     unsigned long long m = 0;
     for (int64_t k = lane; k < K; k += 32) m = max(m, abs_key(p[k * ks]));
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    const int e = key_exp(m, false);
-    for (int64_t k = lane; k < K; k += 32) slice6(p[k * ks], e, dst + r * ld + k, plane);
-    if (lane == 0) {
-      e_out[r] = e;
-      if (scale_out) scale_out[r] = ldexp(1.0, e);
-    }
+    const int e = key_exp(m, float_key<TIn>());
+    for (int64_t k = lane; k < K; k += 32) Put<PR>::put(p[k * ks], e, dst + r * ld + k, plane);
+    if (lane == 0) e_out[r] = e;
   }
 }
 
 // max |X[mu + n r]| over r in [0, nr) per mu (X col-major [n, nr]); atomics per thread
-__global__ void rowmax_strided_kernel(const double* __restrict__ X, int64_t n, int64_t nr,
+template <class TIn>
+__global__ void rowmax_strided_kernel(const TIn* __restrict__ X, int64_t n, int64_t nr,
                                       unsigned long long* __restrict__ mx) {
   const int64_t mu = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (mu >= n) return;
@@ -350,13 +422,14 @@ __global__ void rowmax_strided_kernel(const double* __restrict__ X, int64_t n, i
   atomicMax(mx + mu, m);
 }
 
+// e = exponent of the max; scale = mult 2^(e - eoff)
 __global__ void exp_scale_kernel(const unsigned long long* __restrict__ mx, int64_t n, double mult, bool is_float,
-                                 int* __restrict__ e_out, double* __restrict__ scale) {
+                                 int eoff, int* __restrict__ e_out, double* __restrict__ scale) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int e = key_exp(mx[i], is_float);
   e_out[i] = e;
-  scale[i] = mult * ldexp(1.0, e);
+  scale[i] = mult * ldexp(1.0, e - eoff);
 }
 
 // cderi slices [t][P][mu][ldk] of B_P[mu, nu] 2^-e_mu (B_P symmetric: read Bd[nu + nao mu + nao^2 P])
@@ -371,21 +444,23 @@ __global__ void slice_cderi_kernel(const double* __restrict__ Bd, int64_t nao, i
   }
 }
 
-// Z^T slices [t][P][mu][ldj] of Z_P[mu, j] 2^-e_mu, Z col-major [nao, nocc, naux]
-__global__ void slice_zt_kernel(const double* __restrict__ Z, int64_t nao, int64_t no, int64_t naux, int64_t ldj,
-                                const int* __restrict__ e_row, __nv_bfloat16* __restrict__ out) {
+// Z^T slices [t][P][mu][ldj] of Z_P[mu, j] (row exponent e_mu), Z col-major [nao, nocc, naux]
+template <class PR, class TIn>
+__global__ void slice_zt_kernel(const TIn* __restrict__ Z, int64_t nao, int64_t no, int64_t naux, int64_t ldj,
+                                const int* __restrict__ e_row, typename PR::Elem* __restrict__ out) {
   const int64_t total = nao * no * naux;
   const int64_t plane = naux * nao * ldj;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t mu = t % nao;
     const int64_t r = t / nao;  // j + no * P
     const int64_t j = r % no, P = r / no;
-    slice6(Z[t], e_row[mu], out + j + ldj * (mu + nao * P), plane);
+    Put<PR>::put(Z[t], e_row[mu], out + j + ldj * (mu + nao * P), plane);
   }
 }
 
-// max |hi| of FP32-pair staging rows (Pl, n) of length K (row stride ld) per column n: one warp per row
-__global__ void colmax_pair_kernel(const float2* __restrict__ T, int64_t rows, int64_t N, int64_t ld, int64_t K,
+// max |x| of staging rows (Pl, n) of length K (row stride ld) per column n: one warp per row
+template <class TIn>
+__global__ void colmax_rows_kernel(const TIn* __restrict__ T, int64_t rows, int64_t N, int64_t ld, int64_t K,
                                    unsigned long long* __restrict__ mx) {
   const int lane = threadIdx.x & 31;
   const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -398,15 +473,16 @@ __global__ void colmax_pair_kernel(const float2* __restrict__ T, int64_t rows, i
   }
 }
 
-// slices [t][Pl][n][ld] of the FP32-pair staging T[Pl][n][k] 2^-e_n, k < K
-__global__ void slice_pair_kernel(const float2* __restrict__ T, int64_t rows, int64_t N, int64_t ld, int64_t K,
-                                  const int* __restrict__ e_col, __nv_bfloat16* __restrict__ out) {
+// planes [t][Pl][n][ld] of the staging T[Pl][n][k] with column exponent e_n, k < K
+template <class PR, class TIn>
+__global__ void slice_staging_kernel(const TIn* __restrict__ T, int64_t rows, int64_t N, int64_t ld, int64_t K,
+                                     const int* __restrict__ e_col, typename PR::Elem* __restrict__ out) {
   const int64_t total = rows * K;
   const int64_t plane = rows * ld;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t k = t % K;
     const int64_t r = t / K;
-    slice6(T[r * ld + k], e_col[r % N], out + r * ld + k, plane);
+    Put<PR>::put(T[r * ld + k], e_col[r % N], out + r * ld + k, plane);
   }
 }
 
@@ -431,8 +507,10 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 3-D BF16 tensor map: dims {K, rows, depth}, row stride ld elements, box {32, box_rows, 1}, 64B swizzle.
-CUtensorMap make_map(const void* base, int64_t K, int64_t rows, int64_t depth, int64_t ld, int box_rows) {
+// 3-D BF16 / FP16 tensor map: dims {K, rows, depth}, row stride ld elements, box {32, box_rows, 1},
+// 64B swizzle.
+CUtensorMap make_map(const void* base, int64_t K, int64_t rows, int64_t depth, int64_t ld, int box_rows,
+                     bool bf16 = true) {
   CUtensorMap m;
   std::memset(&m, 0, sizeof(m));
   auto fn = encode_fn();
@@ -441,27 +519,28 @@ CUtensorMap make_map(const void* base, int64_t K, int64_t rows, int64_t depth, i
   cuuint64_t strides[2] = {(cuuint64_t)(ld * 2), (cuuint64_t)(ld * 2 * rows)};
   cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
-  CUresult r = fn(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+  CUresult r = fn(&m, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3,
+                  const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) throw Error(CPHF_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
   return m;
 }
 
-template <int BN, bool BATCHED>
+template <class PR, int BN, bool BATCHED>
 bool set_smem_attr() {
-  return cudaFuncSetAttribute(tc_exact_kernel<BN, BATCHED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              Cfg<BN>::SMEM_BYTES) == cudaSuccess;
+  return cudaFuncSetAttribute(tc_slice_kernel<PR, BN, BATCHED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              Cfg<PR, BN>::SMEM_BYTES) == cudaSuccess;
 }
 
 // split mode: grid (tiles, K ranges = count); batched mode: grid (aux functions = count, tiles)
-template <int BN, bool BATCHED>
-void launch_exact(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, const OzArgs& a, unsigned count) {
+template <class PR, int BN, bool BATCHED>
+void launch_slices(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, const OzArgs& a, unsigned count) {
   const unsigned tiles = (unsigned)(a.m_tiles * div_up(a.N, BN));
   if (tiles > (BATCHED ? 65535u : 0x7FFFFFFFu) || count > (BATCHED ? 0x7FFFFFFFu : 65535u))
     throw Error(CPHF_ERR_ARG, "tensor-core K term: grid too large");
   const dim3 grid = BATCHED ? dim3(count, tiles) : dim3(tiles, count);
-  tc_exact_kernel<BN, BATCHED><<<grid, 128, Cfg<BN>::SMEM_BYTES, c->stream>>>(mA, mB, a);
+  tc_slice_kernel<PR, BN, BATCHED><<<grid, 128, Cfg<PR, BN>::SMEM_BYTES, c->stream>>>(mA, mB, a);
   count_launch();
   CPHF_CUDA(cudaGetLastError());
 }
@@ -485,7 +564,9 @@ bool oz_available(cphf_ctx* c) {
   static bool attr_ok = false, tried = false;
   if (!tried) {
     tried = true;
-    attr_ok = set_smem_attr<128, false>() && set_smem_attr<64, true>() && set_smem_attr<128, true>();
+    attr_ok = set_smem_attr<Exact6, 128, false>() && set_smem_attr<Exact6, 64, true>() &&
+              set_smem_attr<Exact6, 128, true>() && set_smem_attr<Split2, 128, false>() &&
+              set_smem_attr<Split2, 64, true>() && set_smem_attr<Split2, 128, true>();
     if (!attr_ok) cudaGetLastError();
   }
   return attr_ok;
@@ -508,9 +589,9 @@ void oz_prepare_cderi(cphf_ctx* c, OzState& z) {
   CPHF_CUDA(cudaMemsetAsync(z.mx.p, 0, (size_t)nao * 8, c->stream));
   const unsigned gx = (unsigned)div_up(nao, 256);
   const unsigned gy = (unsigned)std::max<int64_t>(1, std::min<int64_t>(nao * naux, 8 * (int64_t)c->num_sms / gx + 1));
-  rowmax_strided_kernel<<<dim3(gx, gy), 256, 0, c->stream>>>(c->Bd.as<double>(), nao, nao * naux,
+  rowmax_strided_kernel<double><<<dim3(gx, gy), 256, 0, c->stream>>>(c->Bd.as<double>(), nao, nao * naux,
                                                               z.mx.as<unsigned long long>());
-  exp_scale_kernel<<<grid_for(nao), 256, 0, c->stream>>>(z.mx.as<unsigned long long>(), nao, 1.0, false,
+  exp_scale_kernel<<<grid_for(nao), 256, 0, c->stream>>>(z.mx.as<unsigned long long>(), nao, 1.0, false, 0,
                                                          z.e_row.as<int>(), z.rowscale.as<double>());
   slice_cderi_kernel<<<grid_for(naux * nao * nao), 256, 0, c->stream>>>(c->Bd.as<double>(), nao, naux, z.ldk,
                                                                         z.e_row.as<int>(), z.A.as<__nv_bfloat16>());
@@ -529,15 +610,13 @@ static void oz_prepare_spin(cphf_ctx* c, OzState& z, int s) {
   // O_P[j, i]: rows (i, P) at O + no (i + no P), K = j
   o.O.ensure((size_t)S * naux * no * ldj * 2, c->counter());
   o.eO.ensure((size_t)naux * no * 4, c->counter());
-  slice_rows_kernel<<<grid_warps(naux * no, c->num_sms), 256, 0, c->stream>>>(
-      sp.O.as<double>(), naux * no, no, 0, no, 0, 1, o.O.as<__nv_bfloat16>(), ldj, naux * no * ldj, o.eO.as<int>(),
-      nullptr);
+  slice_rows_kernel<Exact6, double><<<grid_warps(naux * no, c->num_sms), 256, 0, c->stream>>>(
+      sp.O.as<double>(), naux * no, no, 0, no, 0, 1, o.O.as<__nv_bfloat16>(), ldj, naux * no * ldj, o.eO.as<int>());
   // Z_P[nu, i]: rows (i, P) at Z + nao (i + no P), K = nu
   o.Z.ensure((size_t)S * naux * no * ldk * 2, c->counter());
   o.eZ.ensure((size_t)naux * no * 4, c->counter());
-  slice_rows_kernel<<<grid_warps(naux * no, c->num_sms), 256, 0, c->stream>>>(
-      sp.Z.as<double>(), naux * no, nao, 0, nao, 0, 1, o.Z.as<__nv_bfloat16>(), ldk, naux * no * ldk, o.eZ.as<int>(),
-      nullptr);
+  slice_rows_kernel<Exact6, double><<<grid_warps(naux * no, c->num_sms), 256, 0, c->stream>>>(
+      sp.Z.as<double>(), naux * no, nao, 0, nao, 0, 1, o.Z.as<__nv_bfloat16>(), ldk, naux * no * ldk, o.eZ.as<int>());
   // Z_P[mu, j]: rows mu (scale over all j, P), per-P blocks of K = j
   o.Zt.ensure((size_t)S * naux * nao * ldj * 2, c->counter());
   o.sZt.ensure((size_t)nao * 8, c->counter());
@@ -545,11 +624,11 @@ static void oz_prepare_spin(cphf_ctx* c, OzState& z, int s) {
   CPHF_CUDA(cudaMemsetAsync(z.mx.p, 0, (size_t)nao * 8, c->stream));
   const unsigned gx = (unsigned)div_up(nao, 256);
   const unsigned gy = (unsigned)std::max<int64_t>(1, std::min<int64_t>(no * naux, 8 * (int64_t)c->num_sms / gx + 1));
-  rowmax_strided_kernel<<<dim3(gx, gy), 256, 0, c->stream>>>(sp.Z.as<double>(), nao, no * naux,
+  rowmax_strided_kernel<double><<<dim3(gx, gy), 256, 0, c->stream>>>(sp.Z.as<double>(), nao, no * naux,
                                                               z.mx.as<unsigned long long>());
-  exp_scale_kernel<<<grid_for(nao), 256, 0, c->stream>>>(z.mx.as<unsigned long long>(), nao, 1.0, false,
+  exp_scale_kernel<<<grid_for(nao), 256, 0, c->stream>>>(z.mx.as<unsigned long long>(), nao, 1.0, false, 0,
                                                          o.eZt.as<int>(), o.sZt.as<double>());
-  slice_zt_kernel<<<grid_for(nao * no * naux), 256, 0, c->stream>>>(sp.Z.as<double>(), nao, no, naux, ldj,
+  slice_zt_kernel<Exact6, double><<<grid_for(nao * no * naux), 256, 0, c->stream>>>(sp.Z.as<double>(), nao, no, naux, ldj,
                                                                     o.eZt.as<int>(), o.Zt.as<__nv_bfloat16>());
   count_launch(5);
   CPHF_CUDA(cudaGetLastError());
@@ -569,13 +648,12 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
   // bra slices, both K orders: rows (j, a) over nu (W-gen A) and rows (nu, a) over j (T-gen A)
   z.braw.ensure((size_t)S * N * ldk * 2, c->counter());
   z.ebraw.ensure((size_t)N * 4, c->counter());
-  slice_rows_kernel<<<grid_warps(N, c->num_sms), 256, 0, c->stream>>>(
-      bra, N, nao, 0, nao, 0, 1, z.braw.as<__nv_bfloat16>(), ldk, N * ldk, z.ebraw.as<int>(), nullptr);
+  slice_rows_kernel<Exact6, double><<<grid_warps(N, c->num_sms), 256, 0, c->stream>>>(
+      bra, N, nao, 0, nao, 0, 1, z.braw.as<__nv_bfloat16>(), ldk, N * ldk, z.ebraw.as<int>());
   z.brat.ensure((size_t)S * nao * nb * ldj * 2, c->counter());
   z.ebrat.ensure((size_t)nao * nb * 4, c->counter());
-  slice_rows_kernel<<<grid_warps(nao * nb, c->num_sms), 256, 0, c->stream>>>(
-      bra, nao * nb, no, nao, 1, nao * no, nao, z.brat.as<__nv_bfloat16>(), ldj, nao * nb * ldj, z.ebrat.as<int>(),
-      nullptr);
+  slice_rows_kernel<Exact6, double><<<grid_warps(nao * nb, c->num_sms), 256, 0, c->stream>>>(
+      bra, nao * nb, no, nao, 1, nao * no, nao, z.brat.as<__nv_bfloat16>(), ldj, nao * nb * ldj, z.ebrat.as<int>());
   count_launch(2);
 
   // chunk of aux functions: T staging (FP32 pair, 8 B) + slices (12 B) per element within ~8 GiB
@@ -613,14 +691,14 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
       a.e_col = os.eO.as<int>();
       a.m_div = nao; a.s_m1 = 1; a.s_m2 = ldk * no; a.s_n = ldk; a.s_p = N * ldk;
       ProfScope ps(c, PROF_TC_OZAKI, 2.0 * nao * nb * no * no * npc, 0.0);
-      launch_exact<64, true>(c, mBt, mO, a, (unsigned)npc);
+      launch_slices<Exact6, 64, true>(c, mBt, mO, a, (unsigned)npc);
     }
     CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
-    colmax_pair_kernel<<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
+    colmax_rows_kernel<float2><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
                                                                              z.mxc.as<unsigned long long>());
-    exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true,
+    exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true, 0,
                                                          z.e_col.as<int>(), z.colscale.as<double>());
-    slice_pair_kernel<<<grid_for(rows * nao), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
+    slice_staging_kernel<Exact6, float2><<<grid_for(rows * nao), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
                                                                    z.e_col.as<int>(), z.B.as<__nv_bfloat16>());
     count_launch(3);
     {
@@ -638,7 +716,7 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
       a.colscale = z.colscale.as<double>();
       a.ld_out = nao;
       ProfScope ps(c, PROF_TC_OZAKI, 2.0 * nao * N * nao * npc, 2.0 * S * nao * npc * (nao + N));
-      launch_exact<128, false>(c, mCd, mT, a, (unsigned)div_up(a.total_kb, KB_PER_CTA));
+      launch_slices<Exact6, 128, false>(c, mCd, mT, a, (unsigned)div_up(a.total_kb, KB_PER_CTA));
     }
     {
       // W-gen: W[Pl][(i,a)][j] (FP32 pair), rows m = j + no a, columns i, K = nu
@@ -652,14 +730,14 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
       a.e_col = os.eZ.as<int>();
       a.m_div = no; a.s_m1 = 1; a.s_m2 = ldj * no; a.s_n = ldj; a.s_p = N * ldj;
       ProfScope ps(c, PROF_TC_OZAKI, 2.0 * N * no * nao * npc, 0.0);
-      launch_exact<64, true>(c, mBw, mZ, a, (unsigned)npc);
+      launch_slices<Exact6, 64, true>(c, mBw, mZ, a, (unsigned)npc);
     }
     CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
-    colmax_pair_kernel<<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.W.as<float2>(), rows, N, ldj, no,
+    colmax_rows_kernel<float2><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.W.as<float2>(), rows, N, ldj, no,
                                                                              z.mxc.as<unsigned long long>());
-    exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true,
+    exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true, 0,
                                                          z.e_col.as<int>(), z.colscale.as<double>());
-    slice_pair_kernel<<<grid_for(rows * no), 256, 0, c->stream>>>(z.W.as<float2>(), rows, N, ldj, no,
+    slice_staging_kernel<Exact6, float2><<<grid_for(rows * no), 256, 0, c->stream>>>(z.W.as<float2>(), rows, N, ldj, no,
                                                                    z.e_col.as<int>(), z.Ws.as<__nv_bfloat16>());
     count_launch(3);
     {
@@ -677,13 +755,145 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
       a.colscale = z.colscale.as<double>();
       a.ld_out = nao;
       ProfScope ps(c, PROF_TC_OZAKI, 2.0 * nao * N * no * npc, 2.0 * S * no * npc * (nao + N));
-      launch_exact<128, false>(c, mZt, mW, a, (unsigned)div_up(a.total_kb, KB_PER_CTA));
+      launch_slices<Exact6, 128, false>(c, mZt, mW, a, (unsigned)div_up(a.total_kb, KB_PER_CTA));
     }
   }
   int flag = 0;
   CPHF_CUDA(cudaMemcpyAsync(&flag, z.err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CPHF_CUDA(cudaStreamSynchronize(c->stream));
   if (flag) throw Error(CPHF_ERR_TIMEOUT, "tensor-core FP64 K-term kernel: a bounded pipeline wait expired");
+}
+
+// ---- split-FP16 operator of the inner solves ----------------------------------------------
+// O, Z (K = nu) and Z^T (K = j) split-FP16 planes of one spin, from the FP32 copies
+static void lp_prepare_spin(cphf_ctx* c, OzState& z, int s) {
+  const SpinState& sp = c->spin[s];
+  OzSpin& o = z.spin[s];
+  const int64_t nao = c->nao, naux = c->naux, no = sp.nocc;
+  constexpr int S2 = Split2::S;
+  z.ldk = (nao + 7) / 8 * 8;
+  const int64_t ldk = z.ldk, ldj = o.ldj = (no + 7) / 8 * 8;
+  z.mx.ensure((size_t)std::max<int64_t>(nao, 1) * 8, c->counter());
+  o.O.ensure((size_t)S2 * naux * no * ldj * 2, c->counter());
+  o.eO.ensure((size_t)naux * no * 4, c->counter());
+  slice_rows_kernel<Split2, float><<<grid_warps(naux * no, c->num_sms), 256, 0, c->stream>>>(
+      sp.O32.as<float>(), naux * no, no, 0, no, 0, 1, o.O.as<__half>(), ldj, naux * no * ldj, o.eO.as<int>());
+  o.Z.ensure((size_t)S2 * naux * no * ldk * 2, c->counter());
+  o.eZ.ensure((size_t)naux * no * 4, c->counter());
+  slice_rows_kernel<Split2, float><<<grid_warps(naux * no, c->num_sms), 256, 0, c->stream>>>(
+      sp.Z32.as<float>(), naux * no, nao, 0, nao, 0, 1, o.Z.as<__half>(), ldk, naux * no * ldk, o.eZ.as<int>());
+  o.Zt.ensure((size_t)S2 * naux * nao * ldj * 2, c->counter());
+  o.sZt.ensure((size_t)nao * 8, c->counter());
+  o.eZt.ensure((size_t)nao * 4, c->counter());
+  CPHF_CUDA(cudaMemsetAsync(z.mx.p, 0, (size_t)nao * 8, c->stream));
+  const unsigned gx = (unsigned)div_up(nao, 256);
+  const unsigned gy = (unsigned)std::max<int64_t>(1, std::min<int64_t>(no * naux, 8 * (int64_t)c->num_sms / gx + 1));
+  rowmax_strided_kernel<float><<<dim3(gx, gy), 256, 0, c->stream>>>(sp.Z32.as<float>(), nao, no * naux,
+                                                                     z.mx.as<unsigned long long>());
+  exp_scale_kernel<<<grid_for(nao), 256, 0, c->stream>>>(z.mx.as<unsigned long long>(), nao, 1.0, true,
+                                                         Split2::EOFF, o.eZt.as<int>(), o.sZt.as<double>());
+  slice_zt_kernel<Split2, float><<<grid_for(nao * no * naux), 256, 0, c->stream>>>(
+      sp.Z32.as<float>(), nao, no, naux, ldj, o.eZt.as<int>(), o.Zt.as<__half>());
+  count_launch(5);
+  CPHF_CUDA(cudaGetLastError());
+  o.ready = true;
+}
+
+void lp_begin(cphf_ctx* c, OzState& z, int s, const float* bra, int64_t nb) {
+  if (!z.spin[s].ready) lp_prepare_spin(c, z, s);
+  const int64_t nao = c->nao, no = c->spin[s].nocc, N = no * nb;
+  const int64_t ldk = z.ldk, ldj = z.spin[s].ldj;
+  constexpr int S2 = Split2::S;
+  // rows (j, a) over nu (W-gen A) and rows (nu, a) over j (T-gen A)
+  z.braw.ensure((size_t)S2 * N * ldk * 2, c->counter());
+  z.ebraw.ensure((size_t)N * 4, c->counter());
+  slice_rows_kernel<Split2, float><<<grid_warps(N, c->num_sms), 256, 0, c->stream>>>(
+      bra, N, nao, 0, nao, 0, 1, z.braw.as<__half>(), ldk, N * ldk, z.ebraw.as<int>());
+  z.brat.ensure((size_t)S2 * nao * nb * ldj * 2, c->counter());
+  z.ebrat.ensure((size_t)nao * nb * 4, c->counter());
+  slice_rows_kernel<Split2, float><<<grid_warps(nao * nb, c->num_sms), 256, 0, c->stream>>>(
+      bra, nao * nb, no, nao, 1, nao * no, nao, z.brat.as<__half>(), ldj, nao * nb * ldj, z.ebrat.as<int>());
+  count_launch(2);
+  CPHF_CUDA(cudaGetLastError());
+}
+
+void lp_tgen(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, float* T32, int64_t ldt,
+             int* err) {
+  const int64_t nao = c->nao, naux = c->naux, no = c->spin[s].nocc, N = no * nb;
+  const int64_t ldj = z.spin[s].ldj;
+  constexpr int S2 = Split2::S;
+  const CUtensorMap mBt = make_map(z.brat.p, no, nao * nb, S2, ldj, BM, false);
+  const CUtensorMap mO = make_map(z.spin[s].O.p, no, no, S2 * naux, ldj, 64, false);
+  OzArgs a = base_args(z, (int)(nao * nb), (int)no);
+  a.err = err;
+  a.out = T32;
+  a.nkb = (int)div_up(no, BK);
+  a.a_depth = 1;
+  a.b_depth = (int)naux;
+  a.b_off = (int)P0;
+  a.e_row = z.ebrat.as<int>();
+  a.e_col = z.spin[s].eO.as<int>();
+  a.m_div = nao; a.s_m1 = 1; a.s_m2 = ldt * no; a.s_n = ldt; a.s_p = N * ldt;
+  ProfScope ps(c, PROF_TC_KTERM, 2.0 * nao * nb * no * no * npc, 0.0);
+  launch_slices<Split2, 64, true>(c, mBt, mO, a, (unsigned)npc);
+}
+
+void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, double alpha, float* out,
+                int* err) {
+  const int64_t nao = c->nao, naux = c->naux, no = c->spin[s].nocc, N = no * nb;
+  const int64_t ldk = z.ldk, ldj = z.spin[s].ldj;
+  constexpr int S2 = Split2::S;
+  const OzSpin& os = z.spin[s];
+  z.W.ensure((size_t)npc * N * ldj * 4, c->counter());
+  z.Ws.ensure((size_t)S2 * npc * N * ldj * 2, c->counter());
+  z.colscale.ensure((size_t)N * 8, c->counter());
+  z.e_col.ensure((size_t)N * 4, c->counter());
+  z.mxc.ensure((size_t)N * 8, c->counter());
+  const int64_t rows = npc * N;
+  {
+    // W-gen: W[Pl][(i,a)][j], rows m = j + no a, columns i, K = nu
+    const CUtensorMap mBw = make_map(z.braw.p, nao, N, S2, ldk, BM, false);
+    const CUtensorMap mZ = make_map(os.Z.p, nao, no, S2 * naux, ldk, 64, false);
+    OzArgs a = base_args(z, (int)N, (int)no);
+    a.err = err;
+    a.out = z.W.p;
+    a.nkb = (int)div_up(nao, BK);
+    a.a_depth = 1;
+    a.b_depth = (int)naux;
+    a.b_off = (int)P0;
+    a.e_row = z.ebraw.as<int>();
+    a.e_col = os.eZ.as<int>();
+    a.m_div = no; a.s_m1 = 1; a.s_m2 = ldj * no; a.s_n = ldj; a.s_p = N * ldj;
+    ProfScope ps(c, PROF_TC_KTERM, 2.0 * N * no * nao * npc, 0.0);
+    launch_slices<Split2, 64, true>(c, mBw, mZ, a, (unsigned)npc);
+  }
+  CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
+  colmax_rows_kernel<float><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.W.as<float>(), rows, N, ldj, no,
+                                                                                  z.mxc.as<unsigned long long>());
+  exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true, Split2::EOFF,
+                                                       z.e_col.as<int>(), z.colscale.as<double>());
+  slice_staging_kernel<Split2, float><<<grid_for(rows * no), 256, 0, c->stream>>>(
+      z.W.as<float>(), rows, N, ldj, no, z.e_col.as<int>(), z.Ws.as<__half>());
+  count_launch(3);
+  {
+    // term 2: out[mu, n] += alpha sum_{P, j} Z_P[mu, j] W_P[j, n]
+    const CUtensorMap mZt = make_map(os.Zt.p, no, nao, S2 * naux, ldj, BM, false);
+    const CUtensorMap mW = make_map(z.Ws.p, no, N, S2 * npc, ldj, BM, false);
+    OzArgs a = base_args(z, (int)nao, (int)N);
+    a.err = err;
+    a.out = out;
+    a.nkb = (int)div_up(no, BK);
+    a.total_kb = (int)(npc * a.nkb);
+    a.a_depth = (int)naux;
+    a.a_off = (int)P0;
+    a.a_per_p = 1;
+    a.b_depth = (int)npc;
+    a.rowscale = os.sZt.as<double>();
+    a.colscale = z.colscale.as<double>();
+    a.ld_out = nao;
+    ProfScope ps(c, PROF_TC_KTERM, 2.0 * nao * N * no * npc, 2.0 * S2 * no * npc * (nao + N));
+    launch_slices<Split2, 128, false>(c, mZt, mW, a, (unsigned)div_up(a.total_kb, KB_PER_CTA));
+  }
 }
 
 }  // namespace cphf

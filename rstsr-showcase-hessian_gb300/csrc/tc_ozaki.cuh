@@ -19,4 +19,15 @@ void oz_prepare_cderi(cphf_ctx* c, OzState& z);
 // bra FP64 [nao, nocc_s, nb]
 void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, double alpha, double* out);
 
+// Split-FP16 (hi/lo, three products, FP32 accumulation) contractions of the K term for the
+// inner solves' operator, from the FP32 copies of O and Z:
+// per call, the bra planes of spin s (bra FP32 [nao, nocc_s, nb])
+void lp_begin(cphf_ctx* c, OzState& z, int s, const float* bra, int64_t nb);
+// T[Pl][(i,a)][nu] (FP32, row stride ldt) = sum_j bra[nu,j,a] O_P[j,i] for P in [P0, P0 + npc)
+void lp_tgen(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, float* T32, int64_t ldt,
+             int* err);
+// out (FP32 [nao, nocc_s, nb]) += alpha sum_{P in chunk} Z_P (Z_P^T bra)^T
+void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, double alpha, float* out,
+                int* err);
+
 }  // namespace cphf

@@ -18,6 +18,10 @@ MEDIUM = dict(nao=96, naux=300, nocc=(12,), natm=8, decay=12.0)
 MEDIUM_U = dict(nao=80, naux=260, nocc=(11, 9), natm=6, decay=12.0)
 GRID_R = dict(nao=64, naux=200, nocc=(9,), natm=4, decay=10.0, grid=True, points=(700, 1300), window=20)
 GRID_U = dict(nao=60, naux=180, nocc=(8, 7), natm=4, decay=10.0, grid=True, points=(600, 1100), window=20)
+# Split-FP16 operator of the inner solves (22-bit planes scaled per operand row, FP32
+# accumulation, T and W re-split between contractions): ~1e-6 relative to FP64; its error is
+# removed by the defect correction, whose final accuracy the mixed-solve tests check.
+LOWP_TOL = 1e-5
 
 
 def make_ctx(s, precision="fp64", **cfg):
@@ -128,7 +132,7 @@ def test_xc_response_chunked_grouped(chunk):
     assert rel_err(ctx.get_response_bra(bra, plugin="xc"), ref) < 1e-12
     lp = make_ctx(s, precision="mixed", xc_chunk_points=chunk)
     mo1 = np.random.default_rng(16).standard_normal((s.nao, s.nocc[0], 3))
-    assert rel_err(lp.response_dimless_cphf_lowp(mo1), ctx.response_dimless_cphf(mo1)) < 3e-6
+    assert rel_err(lp.response_dimless_cphf_lowp(mo1), ctx.response_dimless_cphf(mo1)) < LOWP_TOL
 
 
 def test_xc_response_uks():
@@ -211,7 +215,7 @@ TC_RAGGED = dict(nao=150, naux=70, nocc=(13,), natm=9, decay=12.0)
 @pytest.mark.parametrize("tc", [1, 0])
 @pytest.mark.parametrize("dims", [MEDIUM, TC_RAGGED, MEDIUM_U, GRID_R])
 def test_lowp_operator_accuracy(dims, tc):
-    """The split-precision operator of the mixed solve agrees with FP64 to a few 1e-7."""
+    """The split-precision operator of the mixed solve agrees with FP64 to LOWP_TOL."""
     s = synth.make_system(dims, seed=14)
     c64 = make_ctx(s)
     clp = make_ctx(s, precision="mixed", tensor_cores=tc)
@@ -223,7 +227,7 @@ def test_lowp_operator_accuracy(dims, tc):
         mo1 = [rng.standard_normal((s.nao, s.nocc[t], 5)) for t in range(2)]
         ref, got = c64.response_dimless_cphf(mo1), clp.response_dimless_cphf_lowp(mo1)
     for a, b in zip(got, ref):
-        assert rel_err(a, b) < 3e-6
+        assert rel_err(a, b) < LOWP_TOL
 
 
 def _max_col_residual(c64, s, x):
