@@ -323,22 +323,28 @@ def run_gpu(args, world, rank, local):
     # roofline of the dominant kernel class in the timed region
     hbm, bf16, peak_src = load_peaks()
     dom_name, dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    tensor_notes = {
+        "kterm_tcgen05_f16x3": "FP16 hi/lo, the tensor pipe executes 3 split products",
+        "tw_term2_tcgen05_f16x3": "FP16 hi/lo, the tensor pipe executes 3 split products",
+        "kterm_tcgen05_bf16x6_exact": "exact BF16 slices, the tensor pipe executes 21 slice products",
+    }
     if dom_name == "gemm_fp64_simt":
         peak = measure_fp64_peak()
         roof = dict(bound="tensor", achieved=dom["flops"] / dom["ms"] / 1e9, peak=peak, unit="TFLOP/s",
                     peak_source="in-run cuBLAS FP64 GEMM 8192^3 (FP64 has no entry in MEASURED_PEAKS.json)")
-    elif dom_name == "kterm_tcgen05_bf16x6_exact":
-        roof = dict(bound="tensor", achieved=dom["flops"] / dom["ms"] / 1e9, peak=bf16, unit="TFLOP/s",
-                    peak_source=f"{peak_src} bf16 dense; achieved counts the algorithmic FP64 FLOPs, the "
-                                "tensor pipe executes 21 BF16 slice products")
-    elif dom_name == "kterm_tcgen05_f16x3":
-        roof = dict(bound="tensor", achieved=dom["flops"] / dom["ms"] / 1e9, peak=bf16, unit="TFLOP/s",
-                    peak_source=f"{peak_src} bf16 dense (FP16 runs at the same rate); achieved counts "
-                                "algorithmic FLOPs, the tensor pipe executes 3 split products")
     else:
+        note = tensor_notes.get(dom_name, "")
         roof = dict(bound="tensor", achieved=dom["flops"] / dom["ms"] / 1e9, peak=bf16, unit="TFLOP/s",
-                    peak_source=peak_src)
-    roof.update(kernel=dom_name, frac=roof["achieved"] / roof["peak"], traffic=None,
+                    peak_source=f"{peak_src} bf16 dense (FP16 runs at the same rate); achieved counts algorithmic "
+                                f"FLOPs" + (f"; {note}" if note else ""))
+    # DRAM bytes per launch: the ratio of ncu-measured DRAM bytes to the algorithmic bytes of
+    # the same kernel on a small case (profiles/), times this run's algorithmic bytes per launch
+    traffic_ratio = {"kterm_tcgen05_f16x3": 1.262 / 1.18}   # tc_term1_kernel, rhf_nao300
+    traffic = None
+    if dom_name in traffic_ratio and dom.get("bytes", 0) > 0:
+        traffic = traffic_ratio[dom_name] * dom["bytes"] / dom["launches"]
+    roof.update(kernel=dom_name, frac=roof["achieved"] / roof["peak"], traffic=traffic,
+                traffic_unit="bytes per launch" if traffic else None,
                 launches=dom["launches"], avg_launch_ms=dom["ms"] / dom["launches"],
                 share_of_step=dom["ms"] * 1e-3 / (t_step * args.steps))
 

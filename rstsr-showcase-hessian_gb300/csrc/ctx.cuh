@@ -124,7 +124,8 @@ enum ProfClass {
   PROF_TC_KTERM = 2,
   PROF_GEMM_F64E = 3,
   PROF_TC_OZAKI = 4,
-  PROF_NCLASS = 5
+  PROF_TC_SPLIT = 5,
+  PROF_NCLASS = 6
 };
 extern const char* const kProfNames[PROF_NCLASS];
 

@@ -139,9 +139,10 @@ __global__ void __launch_bounds__(128, 1)
     }
     __syncwarp();
     // epilogue: all four warps, warp w owns TMEM lanes [32 w, 32 w + 32)
-    const bool have = mbar_wait(accum, 0, args.err);
+    // warp-uniform decision: tcgen05.ld is a whole-warp instruction
+    const bool have = __all_sync(0xffffffffu, mbar_wait(accum, 0, args.err) && *(volatile int*)args.err == 0);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (have && *(volatile int*)args.err == 0) {
+    if (have) {
       const float scale = *args.scale;
       const int row = m0 + warp * 32 + lane;
       for (int c = 0; c < BN / 32; ++c) {
@@ -190,13 +191,21 @@ __global__ void split_cderi_kernel(const double* __restrict__ Bd, int64_t nao, i
   }
 }
 
-// |x| maxima: one atomicMax on the float bit pattern per block
-// max |x| over rows [0, rows) of length `valid` with row stride `ld` (no per-element division)
+// |x| maxima: one atomicMax on the float bit pattern per warp.
+// max |x| over rows [0, rows) of length `valid` with row stride `ld` (ld % 4 == 0: rows start
+// 16-byte aligned; float4 loads, scalar tail)
 __global__ void absmax_f32_kernel(const float* __restrict__ x, int64_t rows, int64_t ld, int64_t valid,
                                   unsigned* out) {
   float m = 0.f;
-  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x)
-    for (int64_t v = threadIdx.x; v < valid; v += blockDim.x) m = fmaxf(m, fabsf(x[r * ld + v]));
+  const int64_t v4 = valid / 4;
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    const float4* row4 = reinterpret_cast<const float4*>(x + r * ld);
+    for (int64_t v = threadIdx.x; v < v4; v += blockDim.x) {
+      const float4 q = row4[v];
+      m = fmaxf(m, fmaxf(fmaxf(fabsf(q.x), fabsf(q.y)), fmaxf(fabsf(q.z), fabsf(q.w))));
+    }
+    for (int64_t v = 4 * v4 + threadIdx.x; v < valid; v += blockDim.x) m = fmaxf(m, fabsf(x[r * ld + v]));
+  }
   for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
 }
@@ -223,15 +232,19 @@ __global__ void t_scale_kernel(const unsigned* mx, float sA, float alpha, float*
   scale[1] = alpha / (sA * s);
 }
 
-// T32 chunk [np][N][ldk] (FP32) -> planes, nu >= nao skipped (never read: outside the TMA extent)
-__global__ void split_t_kernel(const float* __restrict__ t32, int64_t n, const float* __restrict__ scale,
-                               __half* __restrict__ hi, __half* __restrict__ lo) {
+// T32 chunk [np][N][ldk] (FP32) -> planes, four elements per thread (n % 4 == 0); nu >= nao
+// is split too but never read (outside the TMA extent)
+__global__ void split_t_kernel(const float4* __restrict__ t32, int64_t n4, const float* __restrict__ scale,
+                               uint2* __restrict__ hi, uint2* __restrict__ lo) {
   const float s = scale[0];
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-    const float xs = t32[t] * s;
-    const __half h = __float2half_rn(xs);
-    hi[t] = h;
-    lo[t] = __float2half_rn(xs - __half2float(h));
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n4; t += (int64_t)gridDim.x * blockDim.x) {
+    float4 x = t32[t];
+    x.x *= s; x.y *= s; x.z *= s; x.w *= s;
+    const __half2 h01 = __floats2half2_rn(x.x, x.y), h23 = __floats2half2_rn(x.z, x.w);
+    const float2 f01 = __half22float2(h01), f23 = __half22float2(h23);
+    const __half2 l01 = __floats2half2_rn(x.x - f01.x, x.y - f01.y), l23 = __floats2half2_rn(x.z - f23.x, x.w - f23.y);
+    hi[t] = make_uint2(*reinterpret_cast<const unsigned*>(&h01), *reinterpret_cast<const unsigned*>(&h23));
+    lo[t] = make_uint2(*reinterpret_cast<const unsigned*>(&l01), *reinterpret_cast<const unsigned*>(&l23));
   }
 }
 
@@ -353,7 +366,8 @@ void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, 
     absmax_f32_kernel<<<(unsigned)std::min<int64_t>(npc * N, 8 * (int64_t)c->num_sms), 256, 0, c->stream>>>(
         T32, npc * N, ldk, nao, mx);
     t_scale_kernel<<<1, 1, 0, c->stream>>>(mx, (float)L.sA, (float)alpha, scale);
-    split_t_kernel<<<grid_for(tn), 256, 0, c->stream>>>(T32, tn, scale, Thi.as<__half>(), Tlo.as<__half>());
+    split_t_kernel<<<grid_for(tn / 4), 256, 0, c->stream>>>(reinterpret_cast<const float4*>(T32), tn / 4, scale,
+                                                            Thi.as<uint2>(), Tlo.as<uint2>());
     count_launch(3);
     const CUtensorMap mAh = make_map(Bhi.p, nao, nao, naux, ldk, BM);
     const CUtensorMap mAl = make_map(Blo.p, nao, nao, naux, ldk, BM);

@@ -94,6 +94,7 @@ struct OzArgs {
   int a_depth, b_depth;     // plane stride of A / B in depth units (slice t at depth t * stride)
   int a_off, b_off;         // depth offset of the chunk's aux function 0
   int a_per_p;              // A depth advances with the aux function
+  int np, p_per_cta;        // batched: aux functions of the launch, per CTA
   // split mode epilogue: out [m + ld_out n] += value rowscale[m] colscale[n] (double: Exact6, float: Split2)
   const double* rowscale;
   const double* colscale;
@@ -124,7 +125,8 @@ __device__ __forceinline__ void combine4(float a0, float a1, float a2, float a3,
   lo = e - (hi - s);
 }
 
-template <class PR, int BN, bool BATCHED>
+// Split-K contractions (terms 1 and 2): one CTA per (tile, K range of at most KMAX).
+template <class PR, int BN>
 __global__ void __launch_bounds__(128, 1)
     tc_slice_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB, OzArgs args) {
   using C = Cfg<PR, BN>;
@@ -136,13 +138,11 @@ __global__ void __launch_bounds__(128, 1)
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES), accum = smem_u32(bars + 2 * STAGES);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // split mode: x = tile (M fastest), y = K range; batched mode: x = aux function (CTAs that
-  // share an A tile run together), y = tile
-  const int tile = BATCHED ? (int)blockIdx.y : (int)blockIdx.x;
-  const int m_tile = tile % args.m_tiles, n_tile = tile / args.m_tiles;
+  // x = tile (M fastest: CTAs that share a B tile run together), y = K range
+  const int m_tile = blockIdx.x % args.m_tiles, n_tile = blockIdx.x / args.m_tiles;
   const int m0 = m_tile * BM, n0 = n_tile * BN;
-  const int kb0 = BATCHED ? 0 : blockIdx.y * KB_PER_CTA;
-  const int total = BATCHED ? args.nkb : min(args.total_kb - kb0, KB_PER_CTA);
+  const int kb0 = blockIdx.y * KB_PER_CTA;
+  const int total = min(args.total_kb - kb0, KB_PER_CTA);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -170,8 +170,8 @@ __global__ void __launch_bounds__(128, 1)
         const uint32_t full = full0 + 8 * s;
         mbar_expect_tx(full, C::STAGE_BYTES);
         const int kb = kb0 + it;
-        const int P = BATCHED ? (int)blockIdx.x : kb / args.nkb;
-        const int k0 = (BATCHED ? kb : kb % args.nkb) * BK;
+        const int P = kb / args.nkb;
+        const int k0 = (kb % args.nkb) * BK;
         const int da = args.a_off + (args.a_per_p ? P : 0);
         const int db = args.b_off + P;
         const uint32_t st = smem_u32(smem + s * C::STAGE_BYTES);
@@ -220,25 +220,14 @@ __global__ void __launch_bounds__(128, 1)
       mma_commit(accum);  // arrives when every issued MMA has retired (also after an early exit)
     }
     __syncwarp();
-    const bool have = mbar_wait(accum, 0, args.err);
+    // warp-uniform decision: tcgen05.ld is a whole-warp instruction
+    const bool have = __all_sync(0xffffffffu, mbar_wait(accum, 0, args.err) && *(volatile int*)args.err == 0);
     fence_after_sync();
-    if (have && *(volatile int*)args.err == 0) {
+    if (have) {
       const int row = m0 + warp * 32 + lane;
       const bool row_ok = row < args.M;
       const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-      double rs = 0.0;
-      int erow = 0;
-      int64_t base = 0;
-      const int Pl = BATCHED ? (int)blockIdx.x : 0;
-      if (row_ok) {
-        if (BATCHED) {
-          erow = args.e_row[row];
-          base = args.m_div > 0 ? (row % args.m_div) * args.s_m1 + (row / args.m_div) * args.s_m2 : row * args.s_m1;
-          base += (int64_t)Pl * args.s_p;
-        } else {
-          rs = args.rowscale[row];
-        }
-      }
+      const double rs = row_ok ? args.rowscale[row] : 0.0;
       for (int c = 0; c < BN / 32; ++c) {
         if constexpr (PR::NACC == 4) {
           float v0[32], v1[32], v2[32], v3[32];
@@ -253,14 +242,8 @@ __global__ void __launch_bounds__(128, 1)
               if (n < args.N) {
                 float hi, lo;
                 combine4(v0[j], v1[j], v2[j], v3[j], hi, lo);
-                if (BATCHED) {
-                  const int e = erow + args.e_col[(int64_t)(args.b_off + Pl) * args.N + n] - 2 * PR::EOFF;
-                  reinterpret_cast<float2*>(args.out)[base + n * args.s_n] =
-                      make_float2(ldexpf(hi, e), ldexpf(lo, e));
-                } else {
-                  const double v = ((double)hi + (double)lo) * (rs * args.colscale[n]);
-                  atomicAdd(reinterpret_cast<double*>(args.out) + row + args.ld_out * (int64_t)n, v);
-                }
+                const double v = ((double)hi + (double)lo) * (rs * args.colscale[n]);
+                atomicAdd(reinterpret_cast<double*>(args.out) + row + args.ld_out * (int64_t)n, v);
               }
             }
           }
@@ -271,15 +254,9 @@ __global__ void __launch_bounds__(128, 1)
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
               const int n = n0 + c * 32 + j;
-              if (n < args.N) {
-                if (BATCHED) {
-                  const int e = erow + args.e_col[(int64_t)(args.b_off + Pl) * args.N + n] - 2 * PR::EOFF;
-                  reinterpret_cast<float*>(args.out)[base + n * args.s_n] = ldexpf(v[j], e);
-                } else {
-                  atomicAdd(reinterpret_cast<float*>(args.out) + row + args.ld_out * (int64_t)n,
-                            v[j] * (float)(rs * args.colscale[n]));
-                }
-              }
+              if (n < args.N)
+                atomicAdd(reinterpret_cast<float*>(args.out) + row + args.ld_out * (int64_t)n,
+                          v[j] * (float)(rs * args.colscale[n]));
             }
           }
         }
@@ -290,6 +267,184 @@ __global__ void __launch_bounds__(128, 1)
   __syncthreads();
   fence_after_sync();
   if (warp == 2) tmem_dealloc(tmem, C::TMEM_COLS);
+}
+
+// Batched contractions (T-gen, W-gen): one CTA per (tile, range of aux functions), the A tile
+// shared by the range.  The accumulators are double-buffered in TMEM, so the epilogue of aux
+// function p overlaps the MMAs of p + 1.  Six warps: 0 TMA producer, 1 MMA issuer and TMEM
+// owner, 2-5 epilogue (warp w drains TMEM lanes [32 (w % 4), 32 (w % 4) + 32)).
+template <class PR, int BN>
+__global__ void __launch_bounds__(192, 1)
+    tc_slice_batched_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB,
+                            OzArgs args) {
+  using C = Cfg<PR, BN>;
+  constexpr int STAGES = C::STAGES;
+  constexpr uint32_t ACC = PR::NACC * BN;  // TMEM columns of one accumulator set
+  static_assert(2 * ACC <= 512, "two accumulator sets");
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * C::STAGE_BYTES);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5);
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES);
+  const uint32_t accf0 = smem_u32(bars + 2 * STAGES), acce0 = smem_u32(bars + 2 * STAGES + 2);
+  const uint32_t done = smem_u32(bars + 2 * STAGES + 4);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tile = blockIdx.y;
+  const int m_tile = tile % args.m_tiles, n_tile = tile / args.m_tiles;
+  const int m0 = m_tile * BM, n0 = n_tile * BN;
+  const int p_begin = blockIdx.x * args.p_per_cta;
+  const int nP = min(args.np - p_begin, args.p_per_cta);
+  const int nkb = args.nkb;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(accf0 + 8 * b, 1);  // tcgen05.commit of the MMA issuer
+      mbar_init(acce0 + 8 * b, 4);  // one arrive per epilogue warp
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) tmem_alloc(smem_u32(tmem_slot), 2 * ACC);
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  if (nP > 0) {
+    if (warp == 0 && lane == 0) {
+      // producer: K blocks of every aux function of the range, back to back through the ring
+      const int total = nP * nkb;
+      int issued = 0;
+      for (int it = 0; it < total; ++it) {
+        const int s = it % STAGES;
+        const uint32_t ph = (it / STAGES) & 1;
+        if (!mbar_wait(empty0 + 8 * s, ph ^ 1, args.err)) break;
+        issued = it + 1;
+        const uint32_t full = full0 + 8 * s;
+        mbar_expect_tx(full, C::STAGE_BYTES);
+        const int P = p_begin + it / nkb;
+        const int k0 = (it % nkb) * BK;
+        const int db = args.b_off + P;
+        const uint32_t st = smem_u32(smem + s * C::STAGE_BYTES);
+#pragma unroll
+        for (int t = 0; t < PR::S; ++t) {
+          tma_load_3d(st + t * C::A_TILE, &mA, full, k0, m0, t * args.a_depth + args.a_off);
+          tma_load_3d(st + PR::S * C::A_TILE + t * C::B_TILE, &mB, full, k0, n0, t * args.b_depth + db);
+        }
+      }
+      for (int it = max(0, issued - STAGES); it < issued; ++it)
+        mbar_wait(full0 + 8 * (it % STAGES), (it / STAGES) & 1, nullptr);
+    } else if (warp == 1 && lane == 0) {
+      // MMA issuer
+      constexpr uint32_t idesc = instr_desc_f16(BM, BN, PR::BF16);
+      bool ok = true;
+      for (int p = 0; p < nP && ok; ++p) {
+        const int b = p & 1;
+        if (!mbar_wait(acce0 + 8 * b, ((p >> 1) & 1) ^ 1, args.err)) break;
+        fence_after_sync();
+        const uint32_t acc_base = tmem + (uint32_t)b * ACC;
+        for (int kb = 0; kb < nkb; ++kb) {
+          const int it = p * nkb + kb;
+          const int s = it % STAGES;
+          if (!mbar_wait(full0 + 8 * s, (it / STAGES) & 1, args.err)) { ok = false; break; }
+          fence_after_sync();
+          const uint32_t st = smem_u32(smem + s * C::STAGE_BYTES);
+          const uint32_t sb = st + PR::S * C::A_TILE;
+#pragma unroll
+          for (int k = 0; k < BK / 16; ++k) {
+            const uint64_t dk = (uint64_t)((k * 32) >> 4);
+            if constexpr (PR::NACC == 4) {
+#pragma unroll
+              for (int g = 0; g < PR::S; ++g) {
+#pragma unroll
+                for (int t = 0; t <= g; ++t) {
+                  const int acc = g < 3 ? g : 3;
+                  const bool first = kb == 0 && k == 0 && t == 0 && g <= 3;
+                  mma_f16(acc_base + (uint32_t)(acc * BN), smem_desc<64>(st + t * C::A_TILE) + dk,
+                          smem_desc<64>(sb + (g - t) * C::B_TILE) + dk, idesc, first ? 0u : 1u);
+                }
+              }
+            } else {
+              mma_f16(acc_base, smem_desc<64>(st) + dk, smem_desc<64>(sb) + dk, idesc, (kb > 0 || k > 0) ? 1u : 0u);
+              mma_f16(acc_base, smem_desc<64>(st) + dk, smem_desc<64>(sb + C::B_TILE) + dk, idesc, 1u);
+              mma_f16(acc_base, smem_desc<64>(st + C::A_TILE) + dk, smem_desc<64>(sb) + dk, idesc, 1u);
+            }
+          }
+          mma_commit(empty0 + 8 * s);
+        }
+        if (ok) mma_commit(accf0 + 8 * b);  // accumulator set b complete when these MMAs retire
+      }
+      // every issued MMA has retired before TMEM is released (also after an early exit)
+      mma_commit(done);
+      mbar_wait(done, 0, nullptr);
+    } else if (warp >= 2) {
+      // epilogue
+      const int q = warp & 3;
+      const int row = m0 + q * 32 + lane;
+      const bool row_ok = row < args.M;
+      int erow = 0;
+      int64_t base = 0;
+      if (row_ok) {
+        erow = args.e_row[row];
+        base = args.m_div > 0 ? (row % args.m_div) * args.s_m1 + (row / args.m_div) * args.s_m2 : row * args.s_m1;
+      }
+      for (int p = 0; p < nP; ++p) {
+        const int b = p & 1;
+        // warp-uniform decision: tcgen05.ld is a whole-warp instruction
+        if (!__all_sync(0xffffffffu, mbar_wait(accf0 + 8 * b, (p >> 1) & 1, args.err))) break;
+        fence_after_sync();
+        const int Pl = p_begin + p;
+        const uint32_t lane_base = tmem + (uint32_t)b * ACC + ((uint32_t)(q * 32) << 16);
+        const int* ecol = args.e_col + (int64_t)(args.b_off + Pl) * args.N;
+        const int64_t pbase = base + (int64_t)Pl * args.s_p;
+#pragma unroll 1
+        for (int c = 0; c < BN / 32; ++c) {
+          if constexpr (PR::NACC == 4) {
+            float v0[32], v1[32], v2[32], v3[32];
+            tmem_ld32(lane_base + (uint32_t)(0 * BN + c * 32), v0);
+            tmem_ld32(lane_base + (uint32_t)(1 * BN + c * 32), v1);
+            tmem_ld32(lane_base + (uint32_t)(2 * BN + c * 32), v2);
+            tmem_ld32(lane_base + (uint32_t)(3 * BN + c * 32), v3);
+            if (row_ok) {
+#pragma unroll
+              for (int j = 0; j < 32; ++j) {
+                const int n = n0 + c * 32 + j;
+                if (n < args.N) {
+                  float hi, lo;
+                  combine4(v0[j], v1[j], v2[j], v3[j], hi, lo);
+                  const int e = erow + ecol[n] - 2 * PR::EOFF;
+                  reinterpret_cast<float2*>(args.out)[pbase + n * args.s_n] = make_float2(ldexpf(hi, e), ldexpf(lo, e));
+                }
+              }
+            }
+          } else {
+            float v[32];
+            tmem_ld32(lane_base + (uint32_t)(c * 32), v);
+            if (row_ok) {
+#pragma unroll
+              for (int j = 0; j < 32; ++j) {
+                const int n = n0 + c * 32 + j;
+                if (n < args.N)
+                  reinterpret_cast<float*>(args.out)[pbase + n * args.s_n] = ldexpf(v[j], erow + ecol[n] - 2 * PR::EOFF);
+              }
+            }
+          }
+        }
+        fence_before_sync();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(acce0 + 8 * b);
+      }
+    }
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  if (warp == 1) tmem_dealloc(tmem, 2 * ACC);
 }
 
 // ---- slicing (integer arithmetic on the bit patterns; the FP64 pipe is not used) ----------
@@ -527,20 +682,34 @@ CUtensorMap make_map(const void* base, int64_t K, int64_t rows, int64_t depth, i
   return m;
 }
 
-template <class PR, int BN, bool BATCHED>
+template <class PR, int BN>
 bool set_smem_attr() {
-  return cudaFuncSetAttribute(tc_slice_kernel<PR, BN, BATCHED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              Cfg<PR, BN>::SMEM_BYTES) == cudaSuccess;
+  return cudaFuncSetAttribute(tc_slice_kernel<PR, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              Cfg<PR, BN>::SMEM_BYTES) == cudaSuccess &&
+         cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              Cfg<PR, 64>::SMEM_BYTES) == cudaSuccess;
 }
 
-// split mode: grid (tiles, K ranges = count); batched mode: grid (aux functions = count, tiles)
-template <class PR, int BN, bool BATCHED>
-void launch_slices(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, const OzArgs& a, unsigned count) {
+// split-K contraction: grid (tiles, K ranges)
+template <class PR, int BN>
+void launch_split(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, const OzArgs& a) {
   const unsigned tiles = (unsigned)(a.m_tiles * div_up(a.N, BN));
-  if (tiles > (BATCHED ? 65535u : 0x7FFFFFFFu) || count > (BATCHED ? 0x7FFFFFFFu : 65535u))
-    throw Error(CPHF_ERR_ARG, "tensor-core K term: grid too large");
-  const dim3 grid = BATCHED ? dim3(count, tiles) : dim3(tiles, count);
-  tc_slice_kernel<PR, BN, BATCHED><<<grid, 128, Cfg<PR, BN>::SMEM_BYTES, c->stream>>>(mA, mB, a);
+  const int64_t ranges = div_up(a.total_kb, KB_PER_CTA);
+  if (ranges > 65535) throw Error(CPHF_ERR_ARG, "tensor-core K term: grid too large");
+  tc_slice_kernel<PR, BN><<<dim3(tiles, (unsigned)ranges), 128, Cfg<PR, BN>::SMEM_BYTES, c->stream>>>(mA, mB, a);
+  count_launch();
+  CPHF_CUDA(cudaGetLastError());
+}
+
+// batched contraction over a.np aux functions: grid (aux ranges, tiles); each CTA takes as
+// many aux functions as keep at least two waves of CTAs on the GPU
+template <class PR>
+void launch_batched(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, OzArgs a) {
+  const int64_t tiles = (int64_t)a.m_tiles * div_up(a.N, 64);
+  if (tiles > 65535) throw Error(CPHF_ERR_ARG, "tensor-core K term: grid too large");
+  a.p_per_cta = (int)std::max<int64_t>(1, std::min<int64_t>(a.np, a.np * tiles / (2 * (int64_t)c->num_sms)));
+  const dim3 grid((unsigned)div_up(a.np, a.p_per_cta), (unsigned)tiles);
+  tc_slice_batched_kernel<PR, 64><<<grid, 192, Cfg<PR, 64>::SMEM_BYTES, c->stream>>>(mA, mB, a);
   count_launch();
   CPHF_CUDA(cudaGetLastError());
 }
@@ -564,9 +733,7 @@ bool oz_available(cphf_ctx* c) {
   static bool attr_ok = false, tried = false;
   if (!tried) {
     tried = true;
-    attr_ok = set_smem_attr<Exact6, 128, false>() && set_smem_attr<Exact6, 64, true>() &&
-              set_smem_attr<Exact6, 128, true>() && set_smem_attr<Split2, 128, false>() &&
-              set_smem_attr<Split2, 64, true>() && set_smem_attr<Split2, 128, true>();
+    attr_ok = set_smem_attr<Exact6, 128>() && set_smem_attr<Split2, 128>();
     if (!attr_ok) cudaGetLastError();
   }
   return attr_ok;
@@ -691,7 +858,8 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
       a.e_col = os.eO.as<int>();
       a.m_div = nao; a.s_m1 = 1; a.s_m2 = ldk * no; a.s_n = ldk; a.s_p = N * ldk;
       ProfScope ps(c, PROF_TC_OZAKI, 2.0 * nao * nb * no * no * npc, 0.0);
-      launch_slices<Exact6, 64, true>(c, mBt, mO, a, (unsigned)npc);
+      a.np = (int)npc;
+      launch_batched<Exact6>(c, mBt, mO, a);
     }
     CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
     colmax_rows_kernel<float2><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
@@ -716,7 +884,7 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
       a.colscale = z.colscale.as<double>();
       a.ld_out = nao;
       ProfScope ps(c, PROF_TC_OZAKI, 2.0 * nao * N * nao * npc, 2.0 * S * nao * npc * (nao + N));
-      launch_slices<Exact6, 128, false>(c, mCd, mT, a, (unsigned)div_up(a.total_kb, KB_PER_CTA));
+      launch_split<Exact6, 128>(c, mCd, mT, a);
     }
     {
       // W-gen: W[Pl][(i,a)][j] (FP32 pair), rows m = j + no a, columns i, K = nu
@@ -730,7 +898,8 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
       a.e_col = os.eZ.as<int>();
       a.m_div = no; a.s_m1 = 1; a.s_m2 = ldj * no; a.s_n = ldj; a.s_p = N * ldj;
       ProfScope ps(c, PROF_TC_OZAKI, 2.0 * N * no * nao * npc, 0.0);
-      launch_slices<Exact6, 64, true>(c, mBw, mZ, a, (unsigned)npc);
+      a.np = (int)npc;
+      launch_batched<Exact6>(c, mBw, mZ, a);
     }
     CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
     colmax_rows_kernel<float2><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.W.as<float2>(), rows, N, ldj, no,
@@ -755,7 +924,7 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
       a.colscale = z.colscale.as<double>();
       a.ld_out = nao;
       ProfScope ps(c, PROF_TC_OZAKI, 2.0 * nao * N * no * npc, 2.0 * S * no * npc * (nao + N));
-      launch_slices<Exact6, 128, false>(c, mZt, mW, a, (unsigned)div_up(a.total_kb, KB_PER_CTA));
+      launch_split<Exact6, 128>(c, mZt, mW, a);
     }
   }
   int flag = 0;
@@ -834,8 +1003,9 @@ void lp_tgen(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb
   a.e_row = z.ebrat.as<int>();
   a.e_col = z.spin[s].eO.as<int>();
   a.m_div = nao; a.s_m1 = 1; a.s_m2 = ldt * no; a.s_n = ldt; a.s_p = N * ldt;
-  ProfScope ps(c, PROF_TC_KTERM, 2.0 * nao * nb * no * no * npc, 0.0);
-  launch_slices<Split2, 64, true>(c, mBt, mO, a, (unsigned)npc);
+  ProfScope ps(c, PROF_TC_SPLIT, 2.0 * nao * nb * no * no * npc, 0.0);
+  a.np = (int)npc;
+  launch_batched<Split2>(c, mBt, mO, a);
 }
 
 void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, double alpha, float* out,
@@ -864,8 +1034,9 @@ void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t
     a.e_row = z.ebraw.as<int>();
     a.e_col = os.eZ.as<int>();
     a.m_div = no; a.s_m1 = 1; a.s_m2 = ldj * no; a.s_n = ldj; a.s_p = N * ldj;
-    ProfScope ps(c, PROF_TC_KTERM, 2.0 * N * no * nao * npc, 0.0);
-    launch_slices<Split2, 64, true>(c, mBw, mZ, a, (unsigned)npc);
+    ProfScope ps(c, PROF_TC_SPLIT, 2.0 * N * no * nao * npc, 0.0);
+    a.np = (int)npc;
+    launch_batched<Split2>(c, mBw, mZ, a);
   }
   CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
   colmax_rows_kernel<float><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.W.as<float>(), rows, N, ldj, no,
@@ -891,8 +1062,8 @@ void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t
     a.rowscale = os.sZt.as<double>();
     a.colscale = z.colscale.as<double>();
     a.ld_out = nao;
-    ProfScope ps(c, PROF_TC_KTERM, 2.0 * nao * N * no * npc, 2.0 * S2 * no * npc * (nao + N));
-    launch_slices<Split2, 128, false>(c, mZt, mW, a, (unsigned)div_up(a.total_kb, KB_PER_CTA));
+    ProfScope ps(c, PROF_TC_SPLIT, 2.0 * nao * N * no * npc, 2.0 * S2 * no * npc * (nao + N));
+    launch_split<Split2, 128>(c, mZt, mW, a);
   }
 }
 

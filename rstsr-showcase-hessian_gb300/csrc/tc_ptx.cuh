@@ -23,6 +23,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
 // Bounded parity wait; returns false (and raises *err) when the limit is reached, or false
 // early when another thread has already raised *err.  err == nullptr: the wait ignores
 // other threads' errors and raises nothing (drain of copies still in flight).
