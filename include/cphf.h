@@ -73,6 +73,8 @@ typedef struct cphf_config {
                                 slice products (6 x 6 bits, ~1e-10 relative to the operand row maxima;
                                 default; without tensor cores it behaves as 1).
                                 The final verification (verify_residual) is always native FP64. */
+  int32_t cuda_graphs;       /* mixed: replay each block width's split-precision operator application
+                                from a captured CUDA graph (default 1); bypassed while profiling */
 } cphf_config;
 
 /* Solver statistics (the reference reports them by println!, krylov_block.rs:148-151, 175). */

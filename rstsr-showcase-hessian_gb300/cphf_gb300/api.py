@@ -73,6 +73,7 @@ class Config(ctypes.Structure):
         ("fp64_every_step", ctypes.c_int32),
         ("xc_chunk_points", ctypes.c_int64),
         ("residual_dfloat", ctypes.c_int32),
+        ("cuda_graphs", ctypes.c_int32),
     ]
 
 
@@ -294,8 +295,8 @@ class Context:
 
     def profile_report(self):
         """``{class: {launches, ms, max_ms, flops, bytes}}`` of the recorded launches."""
-        buf = (ProfEntry * 8)()
-        n = self.lib.cphf_ctx_profile_report(self.h, buf, 8)
+        buf = (ProfEntry * 32)()
+        n = self.lib.cphf_ctx_profile_report(self.h, buf, 32)
         if n < 0:
             self._check(ERR_CUDA)
         return {buf[i].name.decode(): dict(launches=buf[i].launches, ms=buf[i].ms, max_ms=buf[i].max_ms,

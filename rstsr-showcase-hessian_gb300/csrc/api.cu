@@ -150,6 +150,7 @@ cphf_status cphf_config_default(cphf_config* cfg) {
   cfg->fp64_every_step = 0;
   cfg->xc_chunk_points = 0;
   cfg->residual_dfloat = 2;
+  cfg->cuda_graphs = 1;
   return CPHF_OK;
 }
 
@@ -352,7 +353,7 @@ cphf_status cphf_xc_set_grid(cphf_ctx* c, const double* ao, const double* weight
     copy_in(c, c->fxc.p, fxc, (size_t)nf * 8);
     CPHF_CUDA(cudaStreamSynchronize(c->stream));
     c->xc_batches = batches;
-    for (auto& pl : c->xc_plan) pl.key[0] = -1;  // chunk plans depend on the batches
+    c->xc_plans.clear();  // chunk plans depend on the batches
     c->ngrids = ngrids;
     c->xc_nspin = nspin;
     c->has_xc = true;

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <stdexcept>
@@ -39,6 +40,13 @@ inline void check_cuda(cudaError_t e, const char* what) {
     if (!(cond)) throw ::cphf::Error(CPHF_ERR_ARG, std::string(msg)); \
   } while (0)
 
+// Bumped whenever a device buffer is (re)allocated or released, or a cached launch plan is
+// rebuilt: a captured CUDA graph bakes in pointers and plan contents and is replayed only
+// while the generation it was captured at is current.
+extern std::atomic<int64_t> g_state_generation;
+inline void bump_generation() { g_state_generation.fetch_add(1, std::memory_order_relaxed); }
+inline int64_t state_generation() { return g_state_generation.load(std::memory_order_relaxed); }
+
 // Owning device allocation; byte size tracked for cphf_ctx_device_bytes.
 struct DevBuf {
   void* p = nullptr;
@@ -52,6 +60,7 @@ struct DevBuf {
     if (p) {
       cudaFree(p);
       if (counter) *counter -= (int64_t)bytes;
+      bump_generation();
     }
     p = nullptr;
     bytes = 0;
@@ -63,6 +72,7 @@ struct DevBuf {
     counter = cnt;
     if (n == 0) return;
     CPHF_CUDA(cudaMalloc(&p, n));
+    bump_generation();
     bytes = n;
     if (counter) *counter += (int64_t)n;
   }

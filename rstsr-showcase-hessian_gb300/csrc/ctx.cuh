@@ -29,9 +29,16 @@ struct OzState {
   OzSpin spin[2];
   // per-call scratch: bra slices (both K orders), T / Wt staging (FP32 pairs) and slices
   DevBuf braw, ebraw, brat, ebrat, T, B, W, Ws;
-  DevBuf colscale, e_col, mxc, err;
+  DevBuf colscale, e_col, mxc, err, tune_out;
   int64_t ldk = 0;
   bool ready = false;
+};
+
+// One captured application of the split-precision operator for block width nb, reading and
+// writing the staging buffers of LowpState (g_x, g_y).
+struct OpGraph {
+  int64_t nb = 0, gen = -1, nodes = 0;
+  cudaGraphExec_t exec = nullptr;
 };
 
 // State of the split-precision operator (mixed.cu).
@@ -46,6 +53,16 @@ struct LowpState {
   DevBuf err;                  // device error flag of the tensor-core kernels (bounded waits)
   double sA = 1.0;             // power-of-two scale of the FP16 cderi planes
   bool use_tc = true;
+  // captured operator applications (cfg.cuda_graphs)
+  std::vector<OpGraph> graphs;
+  DevBuf g_x, g_y;
+  bool graphs_off = false;     // capture failed once: run the operator eagerly from then on
+  void drop_graphs() {
+    for (auto& g : graphs)
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+    graphs.clear();
+  }
+  ~LowpState() { drop_graphs(); }
 };
 
 // Learned initial guess / preconditioner (mlp.cu): weights, Adam moments, scratch.
@@ -125,7 +142,11 @@ enum ProfClass {
   PROF_GEMM_F64E = 3,
   PROF_TC_OZAKI = 4,
   PROF_TC_SPLIT = 5,
-  PROF_NCLASS = 6
+  PROF_SLICE = 6,
+  PROF_KRYLOV = 7,
+  PROF_XC64 = 8,
+  PROF_XC32 = 9,
+  PROF_NCLASS = 10
 };
 extern const char* const kProfNames[PROF_NCLASS];
 
@@ -154,7 +175,7 @@ struct cphf_ctx {
   std::vector<cphf::XcBatch> xc_batches;
   cphf::DevBuf phi, weights, fxc;  // phi: batch blocks [npts_b, nwin_b] (grid fastest)
   cphf::DevBuf phi32;
-  cphf::XcPlan xc_plan[2];         // FP64 / FP32 chunk plans
+  std::vector<std::unique_ptr<cphf::XcPlan>> xc_plans;  // chunk plans, one per (precision, nb, nocc)
 
   // prepared orbitals
   bool prepared = false;
@@ -216,7 +237,11 @@ void xc_prepare(cphf_ctx* c);
 // response_mo / dimensionless operator over the packed Krylov layout
 // x, y: [n, nb] with n = sum_s nmo*nocc_s.
 void response_mo_fp64(cphf_ctx* c, const double* x, int64_t nb, double* resp_mo, bool dimless);
-void response_mo_lowp(cphf_ctx* c, const double* x, int64_t nb, double* resp_mo);
+// check = false: leave out the device error-flag read (a host synchronisation), for capture
+void response_mo_lowp(cphf_ctx* c, const double* x, int64_t nb, double* resp_mo, bool check = true);
+void lowp_check(cphf_ctx* c);
+// response_mo_lowp as the inner solves apply it, replayed from captured CUDA graphs
+void lowp_apply(cphf_ctx* c, const double* x, int64_t nb, double* y);
 int64_t krylov_n(const cphf_ctx* c);
 
 // krylov_block on the device (src/util/krylov_block.rs:39-197)

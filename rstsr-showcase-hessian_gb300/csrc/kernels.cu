@@ -8,6 +8,7 @@
 
 namespace cphf {
 thread_local int64_t* g_launch_counter = nullptr;
+std::atomic<int64_t> g_state_generation{0};
 
 namespace {
 

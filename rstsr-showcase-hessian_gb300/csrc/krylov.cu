@@ -39,7 +39,10 @@ void orth_block(cphf_ctx* c, const KrylovWork& w, double* V, int64_t n, int64_t 
   ip.assign(m, 0.0);
   if (m == 0) return;
   double* ipd = w.part + mgs_partials_size(n, m) + m;  // after partials + coef
-  launch_mgs(V, n, m, lindep, ipd, w.keep, w.part, c->stream);
+  {
+    ProfScope ps(c, PROF_KRYLOV, 0.0, 0.0);
+    launch_mgs(V, n, m, lindep, ipd, w.keep, w.part, c->stream);
+  }
   CPHF_CUDA(cudaMemcpyAsync(keep.data(), w.keep, m * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CPHF_CUDA(cudaMemcpyAsync(ip.data(), ipd, m * 8, cudaMemcpyDeviceToHost, c->stream));
   CPHF_CUDA(cudaStreamSynchronize(c->stream));
@@ -67,7 +70,10 @@ void projected_solve(cphf_ctx* c, const KrylovWork& w, int64_t n, int64_t nd, in
   g.B = b; g.b_k = 1; g.b_n = n;
   g.C = w.gw; g.c_m = 1; g.c_n = nd;
   gemm64(c, g);
-  launch_lu_solve(w.hw, nd, w.gw, nd, nd, nset, w.info, c->stream);
+  {
+    ProfScope ps(c, PROF_KRYLOV, 0.0, 0.0);
+    launch_lu_solve(w.hw, nd, w.gw, nd, nd, nset, w.info, c->stream);
+  }
   int info = 0;
   CPHF_CUDA(cudaMemcpyAsync(&info, w.info, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   GemmDesc x;  // x_out (+)= xs c

@@ -121,8 +121,9 @@ static void rijk_response_lowp(cphf_ctx* c, float* const* bra, int64_t nb, float
         int* err = L.err.as<int>();
         lp_begin(c, L.lp, s, bra[s], nb);
         tc_k_term1(c, L.Bhi, L.Blo, L.ldk, sp.O32.as<float>(), bra[s], no, nb, -c->scale_k, out[s], L.s_Thi,
-                   L.s_Tlo, [&](int64_t P0, int64_t npc, float* T32) {
-                     lp_tgen(c, L.lp, s, P0, npc, nb, T32, L.ldk, err);
+                   L.s_Tlo, [&](int64_t P0, int64_t npc, __half* hi, __half* lo, unsigned* mx, float* scale) {
+                     lp_tgen_planes(c, L.lp, s, P0, npc, nb, L.ldk, hi, lo, mx, scale, (float)L.sA,
+                                    (float)-c->scale_k, err);
                    });
         for (int64_t P0 = 0; P0 < naux; P0 += np_max)
           lp_w_term2(c, L.lp, s, P0, std::min<int64_t>(np_max, naux - P0), nb, -c->scale_k, out[s], err);
@@ -178,7 +179,7 @@ static void xc_response_lowp(cphf_ctx* c, float* const* bra, int64_t nb, float* 
   xc_response_grouped<float>(c, bra, nb, out, accumulate, L.phi32.as<float>(), aobra, L.s_ket, L.s_rho);
 }
 
-void response_mo_lowp(cphf_ctx* c, const double* x, int64_t nb, double* y) {
+void response_mo_lowp(cphf_ctx* c, const double* x, int64_t nb, double* y, bool check) {
   LowpState& L = *c->lowp;
   const int ns = c->nspin;
   const int64_t nao = c->nao, n = krylov_n(c);
@@ -240,12 +241,90 @@ void response_mo_lowp(cphf_ctx* c, const double* x, int64_t nb, double* y) {
     launch_dimless_f32(L.s_y.as<float>(), xs[s], ns == 1 ? n : nmo * no, sp.e.as<double>(), nmo, no, nb,
                        c->cfg.level_shift, yo, n, c->stream);
   }
+  if (check) lowp_check(c);
+}
+
+void lowp_check(cphf_ctx* c) {
+  LowpState& L = *c->lowp;
   if (L.use_tc && c->has_rijk) {
     int flag = 0;
     CPHF_CUDA(cudaMemcpyAsync(&flag, L.err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CPHF_CUDA(cudaStreamSynchronize(c->stream));
     if (flag) throw Error(CPHF_ERR_TIMEOUT, "tensor-core K-term kernel: a bounded pipeline wait expired");
   }
+}
+
+// The split-precision operator as the inner solves apply it.  With cfg.cuda_graphs each block
+// width nb is captured once into a CUDA graph that reads the staging buffer g_x and writes
+// g_y; later applications copy x in, replay the graph and copy y out.  A graph is replayed
+// only while the buffer / plan generation it was captured at is current (it bakes in
+// pointers and plan contents); the first application of a width, and any application after
+// the generation moved, runs eagerly (warming every buffer and plan) and then captures.
+void lowp_apply(cphf_ctx* c, const double* x, int64_t nb, double* y) {
+  LowpState& L = *c->lowp;
+  if (!c->cfg.cuda_graphs || L.graphs_off || c->prof.on) {
+    response_mo_lowp(c, x, nb, y);
+    return;
+  }
+  const int64_t n = krylov_n(c);
+  const size_t bytes = (size_t)n * nb * 8;
+  L.g_x.ensure(bytes, c->counter());
+  L.g_y.ensure(bytes, c->counter());
+  const int64_t gen = state_generation();
+  for (auto& g : L.graphs) {
+    if (g.nb != nb || g.gen != gen) continue;
+    CPHF_CUDA(cudaMemcpyAsync(L.g_x.p, x, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    CPHF_CUDA(cudaGraphLaunch(g.exec, c->stream));
+    CPHF_CUDA(cudaMemcpyAsync(y, L.g_y.p, bytes, cudaMemcpyDeviceToDevice, c->stream));
+    count_launch(g.nodes);
+    lowp_check(c);
+    return;
+  }
+  // stale or missing: drop graphs of older generations, run eagerly, then capture this width
+  std::vector<OpGraph> keep;
+  for (auto& g : L.graphs) {
+    if (g.gen == gen) keep.push_back(g);
+    else if (g.exec) cudaGraphExecDestroy(g.exec);
+  }
+  L.graphs.swap(keep);
+  response_mo_lowp(c, x, nb, y);
+  const int64_t gen0 = state_generation();
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool ok = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  if (ok) {
+    try {
+      response_mo_lowp(c, L.g_x.as<double>(), nb, L.g_y.as<double>(), false);
+    } catch (...) {
+      ok = false;
+    }
+    const bool ended = cudaStreamEndCapture(c->stream, &graph) == cudaSuccess;
+    ok = ok && ended && graph && state_generation() == gen0;
+  }
+  size_t nodes = 0, kernels = 0;
+  if (ok) ok = cudaGraphGetNodes(graph, nullptr, &nodes) == cudaSuccess;
+  if (ok && nodes > 0) {
+    std::vector<cudaGraphNode_t> list(nodes);
+    ok = cudaGraphGetNodes(graph, list.data(), &nodes) == cudaSuccess;
+    for (size_t i = 0; ok && i < nodes; ++i) {
+      cudaGraphNodeType t;
+      if (cudaGraphNodeGetType(list[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++kernels;
+    }
+  }
+  if (ok) ok = cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+  if (graph) cudaGraphDestroy(graph);
+  if (!ok) {
+    cudaGetLastError();
+    if (exec) cudaGraphExecDestroy(exec);
+    L.graphs_off = true;  // run eagerly from now on
+    return;
+  }
+  OpGraph g;
+  g.nb = nb;
+  g.gen = gen0;
+  g.nodes = (int64_t)kernels;
+  g.exec = exec;
+  L.graphs.push_back(g);
 }
 
 bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, double* x, cphf_stats* st,
@@ -277,7 +356,7 @@ bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, d
   const KrylovParams p{c->cfg.inner_tol, c->cfg.cphf_lindep, c->cfg.cphf_max_cycle, c->cfg.cphf_max_space,
                        c->cfg.verbose != 0};
   DeviceOp op = [&](const double* xin, int64_t nb, double* yout) {
-    response_mo_lowp(c, xin, nb, yout);
+    lowp_apply(c, xin, nb, yout);
     if (m) launch_apply_precond(m, xin, yout, n, nb, c->stream);
     st->lowp_matvec_columns += nb;
   };
@@ -317,7 +396,7 @@ bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, d
       c->oz_kterm = false;
       done = res < c->cfg.residual_tol;
     } else {
-      response_mo_lowp(c, dlt, nset, adl);
+      lowp_apply(c, dlt, nset, adl);
       st->lowp_matvec_columns += nset;
       launch_residual_norms(r, dlt, adl, r, n, nset, c->k_norm.as<double>(), c->k_norm.as<double>() + nset, s);
       CPHF_CUDA(cudaMemcpyAsync(h.data(), c->k_norm.p, nset * 8, cudaMemcpyDeviceToHost, s));

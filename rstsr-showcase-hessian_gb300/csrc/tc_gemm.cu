@@ -285,6 +285,12 @@ unsigned grid_for(int64_t total) { return (unsigned)std::max<int64_t>(1, std::mi
 
 }  // namespace
 
+void launch_t_scale(const unsigned* mx, float sA, float alpha, float* scale, cudaStream_t stream) {
+  t_scale_kernel<<<1, 1, 0, stream>>>(mx, sA, alpha, scale);
+  count_launch();
+  CPHF_CUDA(cudaGetLastError());
+}
+
 bool tc_available(cphf_ctx* c) {
   int major = 0, minor = 0;
   cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, c->device);
@@ -328,7 +334,7 @@ void tc_prepare_cderi(cphf_ctx* c, DevBuf& hi, DevBuf& lo, int64_t& ldk) {
 }
 
 void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, const float* O32, const float* bra,
-                int64_t no, int64_t nb, double alpha, float* out, DevBuf& Thi, DevBuf& Tlo, const TGen& tgen) {
+                int64_t no, int64_t nb, double alpha, float* out, DevBuf& Thi, DevBuf& Tlo, const TPlanes& tplanes) {
   LowpState& L = *c->lowp;
   const int64_t nao = c->nao, naux = c->naux;
   const int64_t N = no * nb;
@@ -339,9 +345,11 @@ void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, 
   const size_t plane = (size_t)np * N * ldk * 2;
   Thi.ensure(plane, c->counter());
   Tlo.ensure(plane, c->counter());
-  L.s_acc.ensure((size_t)np * N * ldk * 4 + 64, c->counter());  // T32 staging + scale scratch
+  // T32 staging (only without the fused plane generator) + scale scratch
+  const size_t t32 = tplanes ? 0 : (size_t)np * N * ldk;
+  L.s_acc.ensure(t32 * 4 + 64, c->counter());
   float* T32 = L.s_acc.as<float>();
-  unsigned* mx = reinterpret_cast<unsigned*>(T32 + (size_t)np * N * ldk);
+  unsigned* mx = reinterpret_cast<unsigned*>(T32 + t32);
   float* scale = reinterpret_cast<float*>(mx + 4);
   L.err.ensure(sizeof(int), c->counter());
   const int m_tiles = (int)div_up(nao, BM), n_tiles = (int)div_up(N, BN);
@@ -351,8 +359,9 @@ void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, 
     const int64_t npc = std::min<int64_t>(np, naux - P0);
     // T32[Pl][(i,a)][nu] = sum_j bra[nu, j, a] O_P[j, i]: one tall GEMM per aux function,
     // rows (nu, a) (two-level index), columns i, K = j
-    if (tgen) {
-      tgen(P0, npc, T32);
+    if (tplanes) {
+      // FP16 planes of T and their scale straight from the T generator (no FP32 T in HBM)
+      tplanes(P0, npc, Thi.as<__half>(), Tlo.as<__half>(), mx, scale);
     } else {
       GemmDesc t;
       t.M = nao * nb; t.N = no; t.K = no; t.batch1 = npc;
@@ -360,15 +369,16 @@ void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, 
       t.B = O32 + P0 * no * no; t.b_k = 1; t.b_n = no; t.b_b1 = no * no;
       t.C = T32; t.c_m = 1; t.c_m2 = ldk * no; t.c_n = ldk; t.c_b1 = N * ldk;
       gemm32(c, t);
+      const int64_t tn = npc * N * ldk;
+      ProfScope ps_slice(c, PROF_SLICE, 0.0, 4.0 * npc * N * nao + 12.0 * tn);
+      CPHF_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned), c->stream));
+      absmax_f32_kernel<<<(unsigned)std::min<int64_t>(npc * N, 8 * (int64_t)c->num_sms), 256, 0, c->stream>>>(
+          T32, npc * N, ldk, nao, mx);
+      t_scale_kernel<<<1, 1, 0, c->stream>>>(mx, (float)L.sA, (float)alpha, scale);
+      split_t_kernel<<<grid_for(tn / 4), 256, 0, c->stream>>>(reinterpret_cast<const float4*>(T32), tn / 4, scale,
+                                                              Thi.as<uint2>(), Tlo.as<uint2>());
+      count_launch(3);
     }
-    const int64_t tn = npc * N * ldk;
-    CPHF_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned), c->stream));
-    absmax_f32_kernel<<<(unsigned)std::min<int64_t>(npc * N, 8 * (int64_t)c->num_sms), 256, 0, c->stream>>>(
-        T32, npc * N, ldk, nao, mx);
-    t_scale_kernel<<<1, 1, 0, c->stream>>>(mx, (float)L.sA, (float)alpha, scale);
-    split_t_kernel<<<grid_for(tn / 4), 256, 0, c->stream>>>(reinterpret_cast<const float4*>(T32), tn / 4, scale,
-                                                            Thi.as<uint2>(), Tlo.as<uint2>());
-    count_launch(3);
     const CUtensorMap mAh = make_map(Bhi.p, nao, nao, naux, ldk, BM);
     const CUtensorMap mAl = make_map(Blo.p, nao, nao, naux, ldk, BM);
     const CUtensorMap mBh = make_map(Thi.p, nao, N, npc, ldk, BN);

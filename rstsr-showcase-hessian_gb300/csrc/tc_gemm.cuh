@@ -3,6 +3,8 @@
 // (src/ri_jk/hess_r.rs:168-170), with B and T each split into FP16 hi + lo and the three
 // products hi*hi + hi*lo + lo*hi accumulated in FP32 in tensor memory.
 #pragma once
+#include <cuda_fp16.h>
+
 #include <cstdint>
 #include <functional>
 
@@ -14,12 +16,17 @@ namespace cphf {
 bool tc_available(cphf_ctx* c);
 // FP16 hi/lo copies of the dense cderi, rows of length ldk (K-major for the MMA)
 void tc_prepare_cderi(cphf_ctx* c, DevBuf& hi, DevBuf& lo, int64_t& ldk);
-// T generator: T32[Pl][(i,a)][nu] (row stride ldk) = sum_j bra[nu,j,a] O_P[j,i], P in [P0, P0 + npc)
-using TGen = std::function<void(int64_t P0, int64_t npc, float* T32)>;
+// T plane generator: FP16 hi / lo planes [Pl][(i,a)][nu] (row stride ldk) of s T_P,
+// T_P[nu, (i,a)] = sum_j bra[nu,j,a] O_P[j,i] for P in [P0, P0 + npc), with *mx = max |T| (float
+// bits) and scale[0] = s, scale[1] = alpha / (sA s) as launch_t_scale writes them
+using TPlanes =
+    std::function<void(int64_t P0, int64_t npc, __half* hi, __half* lo, unsigned* mx, float* scale)>;
 // out (FP32 [nao, nocc, nb]) += alpha * sum_P B_P bra O_P; bra FP32 [nao, nocc, nb], O32 [nocc, nocc, naux];
-// T is made by `tgen` when given, else by an FP32 CUDA-core GEMM
+// T comes from `tplanes` when given, else from an FP32 CUDA-core GEMM, a max and a split
 void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, const float* O32,
                 const float* bra, int64_t nocc, int64_t nb, double alpha, float* out, DevBuf& Thi,
-                DevBuf& Tlo, const TGen& tgen = TGen());
+                DevBuf& Tlo, const TPlanes& tplanes = TPlanes());
+// scale[0] = 2^(14 - e) for max |T| = *mx < 2^e, scale[1] = alpha / (sA scale[0])
+void launch_t_scale(const unsigned* mx, float sA, float alpha, float* scale, cudaStream_t stream);
 
 }  // namespace cphf

@@ -45,9 +45,13 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <type_traits>
 
 #include "kernels.cuh"
+#include "tc_gemm.cuh"
 #include "tc_ozaki.cuh"
 #include "tc_ptx.cuh"
 
@@ -80,7 +84,6 @@ struct Cfg {
   static constexpr int STAGES = PR::STAGES;
   static constexpr int STAGE_BYTES = PR::S * (A_TILE + B_TILE);
   static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*barriers*/ + 1024 /*alignment*/;
-  static constexpr uint32_t TMEM_COLS = PR::NACC * BN;       // one accumulator per group
   static_assert(BN == 64 || BN == 128, "tile width");
   static_assert(SMEM_BYTES <= 232448, "shared memory");
 };
@@ -95,6 +98,12 @@ struct OzArgs {
   int a_off, b_off;         // depth offset of the chunk's aux function 0
   int a_per_p;              // A depth advances with the aux function
   int np, p_per_cta;        // batched: aux functions of the launch, per CTA
+  int kb_per_cta;           // split: K blocks per CTA (<= KMAX / BK, the exactness bound)
+  // batched split-FP16 T generation fused with the FP16 split of T (tc_gemm.cu's term 1):
+  // pass 1 takes max |T| into *mx (float bits), pass 2 writes hi / lo planes of T * (*tscale)
+  unsigned* mx;
+  const float* tscale;
+  void* out_lo;             // the lo plane (same layout as out, the hi plane)
   // split mode epilogue: out [m + ld_out n] += value rowscale[m] colscale[n] (double: Exact6, float: Split2)
   const double* rowscale;
   const double* colscale;
@@ -141,8 +150,8 @@ __global__ void __launch_bounds__(128, 1)
   // x = tile (M fastest: CTAs that share a B tile run together), y = K range
   const int m_tile = blockIdx.x % args.m_tiles, n_tile = blockIdx.x / args.m_tiles;
   const int m0 = m_tile * BM, n0 = n_tile * BN;
-  const int kb0 = blockIdx.y * KB_PER_CTA;
-  const int total = min(args.total_kb - kb0, KB_PER_CTA);
+  const int kb0 = blockIdx.y * args.kb_per_cta;
+  const int total = min(args.total_kb - kb0, args.kb_per_cta);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -152,7 +161,8 @@ __global__ void __launch_bounds__(128, 1)
     mbar_init(accum, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 2) tmem_alloc(smem_u32(tmem_slot), C::TMEM_COLS);
+  constexpr uint32_t TMEM_COLS = PR::NACC * BN;  // one accumulator per group
+  if (warp == 2) tmem_alloc(smem_u32(tmem_slot), TMEM_COLS);
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
@@ -266,19 +276,38 @@ __global__ void __launch_bounds__(128, 1)
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
-  if (warp == 2) tmem_dealloc(tmem, C::TMEM_COLS);
+  if (warp == 2) tmem_dealloc(tmem, TMEM_COLS);
 }
 
 // Batched contractions (T-gen, W-gen): one CTA per (tile, range of aux functions), the A tile
 // shared by the range.  The accumulators are double-buffered in TMEM, so the epilogue of aux
-// function p overlaps the MMAs of p + 1.  Six warps: 0 TMA producer, 1 MMA issuer and TMEM
-// owner, 2-5 epilogue (warp w drains TMEM lanes [32 (w % 4), 32 (w % 4) + 32)).
-template <class PR, int BN>
-__global__ void __launch_bounds__(192, 1)
+// function p overlaps the MMAs of p + 1.  Ten warps: 0 TMA producer, 1 MMA issuer and TMEM
+// owner, 2-9 epilogue (warp w drains TMEM lanes [32 (w % 4), 32 (w % 4) + 32) and column half
+// (w - 2) / 4 of the 64-column tile).
+template <class PR>
+struct Batched {
+  static constexpr int BN = 64;
+  static constexpr int STAGES = PR::S == 6 ? 2 : 3;  // split FP16: small stages, 2-3 CTAs per SM
+  static constexpr int THREADS = 320;
+  static constexpr int EPI_WARPS = 8;
+  static constexpr int SMEM_BYTES = STAGES * Cfg<PR, BN>::STAGE_BYTES + 1024 + 1024;
+};
+
+// 2^e as a float (exact); ldexpf outside the normal range
+__device__ __forceinline__ float pow2f(int e) {
+  return (e >= -126 && e <= 127) ? __int_as_float((e + 127) << 23) : ldexpf(1.f, e);
+}
+
+// EPI: 0 store the scaled values (T / W staging), 1 max |value| only, 2 FP16 hi / lo planes
+enum { EPI_STORE = 0, EPI_MAX = 1, EPI_SPLIT16 = 2 };
+
+template <class PR, int BN, int EPI = EPI_STORE>
+__global__ void __launch_bounds__(320, PR::S == 6 ? 1 : 2)
     tc_slice_batched_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB,
                             OzArgs args) {
   using C = Cfg<PR, BN>;
-  constexpr int STAGES = C::STAGES;
+  static_assert(BN == Batched<PR>::BN, "batched tile width");
+  constexpr int STAGES = Batched<PR>::STAGES;
   constexpr uint32_t ACC = PR::NACC * BN;  // TMEM columns of one accumulator set
   static_assert(2 * ACC <= 512, "two accumulator sets");
   extern __shared__ uint8_t smem_raw[];
@@ -304,7 +333,7 @@ __global__ void __launch_bounds__(192, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(accf0 + 8 * b, 1);  // tcgen05.commit of the MMA issuer
-      mbar_init(acce0 + 8 * b, 4);  // one arrive per epilogue warp
+      mbar_init(acce0 + 8 * b, Batched<PR>::EPI_WARPS);  // one arrive per epilogue warp
     }
     mbar_init(done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -383,16 +412,18 @@ __global__ void __launch_bounds__(192, 1)
       mma_commit(done);
       mbar_wait(done, 0, nullptr);
     } else if (warp >= 2) {
-      // epilogue
+      // epilogue: TMEM lane quarter q, 32-column chunk c
       const int q = warp & 3;
+      const int c = (warp - 2) >> 2;
       const int row = m0 + q * 32 + lane;
       const bool row_ok = row < args.M;
       int erow = 0;
       int64_t base = 0;
       if (row_ok) {
-        erow = args.e_row[row];
+        erow = args.e_row[row] - 2 * PR::EOFF;
         base = args.m_div > 0 ? (row % args.m_div) * args.s_m1 + (row / args.m_div) * args.s_m2 : row * args.s_m1;
       }
+      const int ncol = n0 + c * 32 + lane;  // the column whose exponent this lane fetches
       for (int p = 0; p < nP; ++p) {
         const int b = p & 1;
         // warp-uniform decision: tcgen05.ld is a whole-warp instruction
@@ -400,39 +431,50 @@ __global__ void __launch_bounds__(192, 1)
         fence_after_sync();
         const int Pl = p_begin + p;
         const uint32_t lane_base = tmem + (uint32_t)b * ACC + ((uint32_t)(q * 32) << 16);
-        const int* ecol = args.e_col + (int64_t)(args.b_off + Pl) * args.N;
+        const int ec = ncol < args.N ? args.e_col[(int64_t)(args.b_off + Pl) * args.N + ncol] : 0;
         const int64_t pbase = base + (int64_t)Pl * args.s_p;
-#pragma unroll 1
-        for (int c = 0; c < BN / 32; ++c) {
-          if constexpr (PR::NACC == 4) {
-            float v0[32], v1[32], v2[32], v3[32];
-            tmem_ld32(lane_base + (uint32_t)(0 * BN + c * 32), v0);
-            tmem_ld32(lane_base + (uint32_t)(1 * BN + c * 32), v1);
-            tmem_ld32(lane_base + (uint32_t)(2 * BN + c * 32), v2);
-            tmem_ld32(lane_base + (uint32_t)(3 * BN + c * 32), v3);
-            if (row_ok) {
+        if constexpr (PR::NACC == 4) {
+          float v0[32], v1[32], v2[32], v3[32];
+          tmem_ld32(lane_base + (uint32_t)(0 * BN + c * 32), v0);
+          tmem_ld32(lane_base + (uint32_t)(1 * BN + c * 32), v1);
+          tmem_ld32(lane_base + (uint32_t)(2 * BN + c * 32), v2);
+          tmem_ld32(lane_base + (uint32_t)(3 * BN + c * 32), v3);
 #pragma unroll
-              for (int j = 0; j < 32; ++j) {
-                const int n = n0 + c * 32 + j;
-                if (n < args.N) {
-                  float hi, lo;
-                  combine4(v0[j], v1[j], v2[j], v3[j], hi, lo);
-                  const int e = erow + ecol[n] - 2 * PR::EOFF;
-                  reinterpret_cast<float2*>(args.out)[pbase + n * args.s_n] = make_float2(ldexpf(hi, e), ldexpf(lo, e));
-                }
+          for (int j = 0; j < 32; ++j) {
+            const int n = n0 + c * 32 + j;
+            const float f = pow2f(erow + __shfl_sync(0xffffffffu, ec, j));
+            if (row_ok && n < args.N) {
+              float hi, lo;
+              combine4(v0[j], v1[j], v2[j], v3[j], hi, lo);
+              reinterpret_cast<float2*>(args.out)[pbase + n * args.s_n] = make_float2(hi * f, lo * f);
+            }
+          }
+        } else {
+          float v[32];
+          tmem_ld32(lane_base + (uint32_t)(c * 32), v);
+          float mx = 0.f;
+          const float ts = EPI == EPI_SPLIT16 ? *args.tscale : 1.f;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int n = n0 + c * 32 + j;
+            const float f = pow2f(erow + __shfl_sync(0xffffffffu, ec, j));
+            if (row_ok && n < args.N) {
+              if constexpr (EPI == EPI_STORE) {
+                reinterpret_cast<float*>(args.out)[pbase + n * args.s_n] = v[j] * f;
+              } else if constexpr (EPI == EPI_MAX) {
+                mx = fmaxf(mx, fabsf(v[j] * f));
+              } else {
+                const float x = (v[j] * f) * ts;
+                const __half h = __float2half_rn(x);
+                const int64_t off = pbase + n * args.s_n;
+                reinterpret_cast<__half*>(args.out)[off] = h;
+                reinterpret_cast<__half*>(args.out_lo)[off] = __float2half_rn(x - __half2float(h));
               }
             }
-          } else {
-            float v[32];
-            tmem_ld32(lane_base + (uint32_t)(c * 32), v);
-            if (row_ok) {
-#pragma unroll
-              for (int j = 0; j < 32; ++j) {
-                const int n = n0 + c * 32 + j;
-                if (n < args.N)
-                  reinterpret_cast<float*>(args.out)[pbase + n * args.s_n] = ldexpf(v[j], erow + ecol[n] - 2 * PR::EOFF);
-              }
-            }
+          }
+          if constexpr (EPI == EPI_MAX) {
+            for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            if (lane == 0) atomicMax(args.mx, __float_as_uint(mx));
           }
         }
         fence_before_sync();
@@ -687,31 +729,130 @@ bool set_smem_attr() {
   return cudaFuncSetAttribute(tc_slice_kernel<PR, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               Cfg<PR, BN>::SMEM_BYTES) == cudaSuccess &&
          cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              Cfg<PR, 64>::SMEM_BYTES) == cudaSuccess;
+                              Batched<PR>::SMEM_BYTES) == cudaSuccess &&
+         (PR::S == 6 ||
+          (cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64, EPI_MAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                Batched<PR>::SMEM_BYTES) == cudaSuccess &&
+           cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64, EPI_SPLIT16>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, Batched<PR>::SMEM_BYTES) == cudaSuccess));
+}
+
+// ---- launch-shape autotuner ---------------------------------------------------------------
+// The first eager launch of each contraction shape times the candidate launch shapes with CUDA
+// events and keeps the fastest for the process: K blocks per CTA for the split-K kernels
+// (atomics into the output against parallelism; all within the exactness bound) and aux
+// functions per CTA for the batched kernels (CTA count in waves of the SM count).  Not during
+// stream capture, where the cached (or default) shape is used.
+struct TuneKey {
+  int kind;
+  int64_t M, N, nkb, np;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(kind, M, N, nkb, np) < std::tie(o.kind, o.M, o.N, o.nkb, o.np);
+  }
+};
+struct TuneTable {
+  std::mutex mu;
+  std::map<TuneKey, int> best;
+  bool find(const TuneKey& k, int& v) {
+    std::lock_guard<std::mutex> g(mu);
+    auto it = best.find(k);
+    if (it == best.end()) return false;
+    v = it->second;
+    return true;
+  }
+  void put(const TuneKey& k, int v) {
+    std::lock_guard<std::mutex> g(mu);
+    best[k] = v;
+  }
+};
+TuneTable& tune_table() {
+  static TuneTable t;
+  return t;
+}
+bool capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(s, &st) != cudaSuccess || st != cudaStreamCaptureStatusNone;
+}
+template <class F>
+float time_launch(cudaStream_t s, F&& launch) {
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, s);
+  launch();
+  cudaEventRecord(e1, s);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms;
 }
 
 // split-K contraction: grid (tiles, K ranges)
 template <class PR, int BN>
-void launch_split(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, const OzArgs& a) {
+void launch_split_raw(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, const OzArgs& a) {
   const unsigned tiles = (unsigned)(a.m_tiles * div_up(a.N, BN));
-  const int64_t ranges = div_up(a.total_kb, KB_PER_CTA);
+  const int64_t ranges = div_up(a.total_kb, a.kb_per_cta);
   if (ranges > 65535) throw Error(CPHF_ERR_ARG, "tensor-core K term: grid too large");
   tc_slice_kernel<PR, BN><<<dim3(tiles, (unsigned)ranges), 128, Cfg<PR, BN>::SMEM_BYTES, c->stream>>>(mA, mB, a);
   count_launch();
   CPHF_CUDA(cudaGetLastError());
 }
 
-// batched contraction over a.np aux functions: grid (aux ranges, tiles); each CTA takes as
-// many aux functions as keep at least two waves of CTAs on the GPU
-template <class PR>
-void launch_batched(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, OzArgs a) {
+template <class PR, int BN>
+void launch_split(cphf_ctx* c, OzState& z, const CUtensorMap& mA, const CUtensorMap& mB, OzArgs a) {
+  const TuneKey key{PR::S * 1000 + BN, a.M, a.N, a.nkb, a.total_kb};
+  auto& tab = tune_table();
+  int best = KB_PER_CTA;
+  if (!tab.find(key, best) && !capturing(c->stream)) {
+    // candidates run into a scratch output (the real one accumulates)
+    const size_t esize = PR::NACC == 4 ? 8 : 4;
+    const size_t bytes = (size_t)a.ld_out * a.N * esize;
+    z.tune_out.ensure(bytes, c->counter());
+    OzArgs t = a;
+    t.out = z.tune_out.p;
+    float best_ms = 0.f;
+    for (int kb : {KB_PER_CTA, KB_PER_CTA / 2, KB_PER_CTA / 3}) {
+      t.kb_per_cta = kb;
+      if (div_up(t.total_kb, kb) > 65535) continue;
+      const float ms = time_launch(c->stream, [&] { launch_split_raw<PR, BN>(c, mA, mB, t); });
+      if (best_ms == 0.f || ms < best_ms) best_ms = ms, best = kb;
+    }
+    tab.put(key, best);
+  }
+  a.kb_per_cta = best;
+  launch_split_raw<PR, BN>(c, mA, mB, a);
+}
+
+// batched contraction over a.np aux functions: grid (aux ranges, tiles)
+template <class PR, int EPI>
+void launch_batched_raw(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, OzArgs a, int waves) {
   const int64_t tiles = (int64_t)a.m_tiles * div_up(a.N, 64);
   if (tiles > 65535) throw Error(CPHF_ERR_ARG, "tensor-core K term: grid too large");
-  a.p_per_cta = (int)std::max<int64_t>(1, std::min<int64_t>(a.np, a.np * tiles / (2 * (int64_t)c->num_sms)));
+  a.p_per_cta = (int)std::max<int64_t>(1, std::min<int64_t>(a.np, a.np * tiles / (waves * (int64_t)c->num_sms)));
   const dim3 grid((unsigned)div_up(a.np, a.p_per_cta), (unsigned)tiles);
-  tc_slice_batched_kernel<PR, 64><<<grid, 192, Cfg<PR, 64>::SMEM_BYTES, c->stream>>>(mA, mB, a);
+  tc_slice_batched_kernel<PR, 64, EPI><<<grid, Batched<PR>::THREADS, Batched<PR>::SMEM_BYTES, c->stream>>>(mA, mB, a);
   count_launch();
   CPHF_CUDA(cudaGetLastError());
+}
+
+template <class PR, int EPI = EPI_STORE>
+void launch_batched(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, const OzArgs& a) {
+  const TuneKey key{PR::S * 1000 + 64 + 100 * EPI, a.M, a.N, a.nkb, a.np};
+  auto& tab = tune_table();
+  int best = 2;
+  if (!tab.find(key, best) && !capturing(c->stream)) {
+    // every candidate writes the same staging values: time them on the real output
+    float best_ms = 0.f;
+    for (int w : {2, 4, 8}) {
+      const float ms = time_launch(c->stream, [&] { launch_batched_raw<PR, EPI>(c, mA, mB, a, w); });
+      if (best_ms == 0.f || ms < best_ms) best_ms = ms, best = w;
+    }
+    tab.put(key, best);
+    return;  // the last candidate already wrote the output
+  }
+  launch_batched_raw<PR, EPI>(c, mA, mB, a, best);
 }
 
 OzArgs base_args(OzState& z, int M, int N) {
@@ -720,6 +861,7 @@ OzArgs base_args(OzState& z, int M, int N) {
   a.M = M;
   a.N = N;
   a.m_tiles = (int)div_up(M, BM);
+  a.kb_per_cta = KB_PER_CTA;
   a.err = z.err.as<int>();
   return a;
 }
@@ -815,13 +957,16 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
   // bra slices, both K orders: rows (j, a) over nu (W-gen A) and rows (nu, a) over j (T-gen A)
   z.braw.ensure((size_t)S * N * ldk * 2, c->counter());
   z.ebraw.ensure((size_t)N * 4, c->counter());
-  slice_rows_kernel<Exact6, double><<<grid_warps(N, c->num_sms), 256, 0, c->stream>>>(
-      bra, N, nao, 0, nao, 0, 1, z.braw.as<__nv_bfloat16>(), ldk, N * ldk, z.ebraw.as<int>());
-  z.brat.ensure((size_t)S * nao * nb * ldj * 2, c->counter());
-  z.ebrat.ensure((size_t)nao * nb * 4, c->counter());
-  slice_rows_kernel<Exact6, double><<<grid_warps(nao * nb, c->num_sms), 256, 0, c->stream>>>(
-      bra, nao * nb, no, nao, 1, nao * no, nao, z.brat.as<__nv_bfloat16>(), ldj, nao * nb * ldj, z.ebrat.as<int>());
-  count_launch(2);
+  {
+    ProfScope ps_slice(c, PROF_SLICE, 0.0, 16.0 * N * nao + 12.0 * N * ldk + 12.0 * nao * nb * ldj);
+    slice_rows_kernel<Exact6, double><<<grid_warps(N, c->num_sms), 256, 0, c->stream>>>(
+        bra, N, nao, 0, nao, 0, 1, z.braw.as<__nv_bfloat16>(), ldk, N * ldk, z.ebraw.as<int>());
+    z.brat.ensure((size_t)S * nao * nb * ldj * 2, c->counter());
+    z.ebrat.ensure((size_t)nao * nb * 4, c->counter());
+    slice_rows_kernel<Exact6, double><<<grid_warps(nao * nb, c->num_sms), 256, 0, c->stream>>>(
+        bra, nao * nb, no, nao, 1, nao * no, nao, z.brat.as<__nv_bfloat16>(), ldj, nao * nb * ldj, z.ebrat.as<int>());
+    count_launch(2);
+  }
 
   // chunk of aux functions: T staging (FP32 pair, 8 B) + slices (12 B) per element within ~8 GiB
   int64_t np = std::max<int64_t>(1, (int64_t(8) << 30) / std::max<int64_t>(20 * N * ldk, 1));
@@ -861,14 +1006,17 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
       a.np = (int)npc;
       launch_batched<Exact6>(c, mBt, mO, a);
     }
-    CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
-    colmax_rows_kernel<float2><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
-                                                                             z.mxc.as<unsigned long long>());
-    exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true, 0,
-                                                         z.e_col.as<int>(), z.colscale.as<double>());
-    slice_staging_kernel<Exact6, float2><<<grid_for(rows * nao), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
-                                                                   z.e_col.as<int>(), z.B.as<__nv_bfloat16>());
-    count_launch(3);
+    {
+      ProfScope ps_slice(c, PROF_SLICE, 0.0, (double)rows * (16.0 * nao + 12.0 * ldk));
+      CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
+      colmax_rows_kernel<float2><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
+                                                                               z.mxc.as<unsigned long long>());
+      exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true, 0,
+                                                           z.e_col.as<int>(), z.colscale.as<double>());
+      slice_staging_kernel<Exact6, float2><<<grid_for(rows * nao), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
+                                                                     z.e_col.as<int>(), z.B.as<__nv_bfloat16>());
+      count_launch(3);
+    }
     {
       // term 1: out[mu, n] += alpha sum_{P, nu} B_P[mu, nu] T_P[nu, n]
       const CUtensorMap mT = make_map(z.B.p, nao, N, S * npc, ldk, BM);
@@ -884,7 +1032,7 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
       a.colscale = z.colscale.as<double>();
       a.ld_out = nao;
       ProfScope ps(c, PROF_TC_OZAKI, 2.0 * nao * N * nao * npc, 2.0 * S * nao * npc * (nao + N));
-      launch_split<Exact6, 128>(c, mCd, mT, a);
+      launch_split<Exact6, 128>(c, z, mCd, mT, a);
     }
     {
       // W-gen: W[Pl][(i,a)][j] (FP32 pair), rows m = j + no a, columns i, K = nu
@@ -901,14 +1049,17 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
       a.np = (int)npc;
       launch_batched<Exact6>(c, mBw, mZ, a);
     }
-    CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
-    colmax_rows_kernel<float2><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.W.as<float2>(), rows, N, ldj, no,
-                                                                             z.mxc.as<unsigned long long>());
-    exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true, 0,
-                                                         z.e_col.as<int>(), z.colscale.as<double>());
-    slice_staging_kernel<Exact6, float2><<<grid_for(rows * no), 256, 0, c->stream>>>(z.W.as<float2>(), rows, N, ldj, no,
-                                                                   z.e_col.as<int>(), z.Ws.as<__nv_bfloat16>());
-    count_launch(3);
+    {
+      ProfScope ps_slice(c, PROF_SLICE, 0.0, (double)rows * (16.0 * no + 12.0 * ldj));
+      CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
+      colmax_rows_kernel<float2><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.W.as<float2>(), rows, N, ldj, no,
+                                                                               z.mxc.as<unsigned long long>());
+      exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true, 0,
+                                                           z.e_col.as<int>(), z.colscale.as<double>());
+      slice_staging_kernel<Exact6, float2><<<grid_for(rows * no), 256, 0, c->stream>>>(z.W.as<float2>(), rows, N, ldj, no,
+                                                                     z.e_col.as<int>(), z.Ws.as<__nv_bfloat16>());
+      count_launch(3);
+    }
     {
       // term 2: out[mu, n] += alpha sum_{P, j} Z_P[mu, j] W_P[j, n]
       const CUtensorMap mW = make_map(z.Ws.p, no, N, S * npc, ldj, BM);
@@ -924,7 +1075,7 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
       a.colscale = z.colscale.as<double>();
       a.ld_out = nao;
       ProfScope ps(c, PROF_TC_OZAKI, 2.0 * nao * N * no * npc, 2.0 * S * no * npc * (nao + N));
-      launch_split<Exact6, 128>(c, mZt, mW, a);
+      launch_split<Exact6, 128>(c, z, mZt, mW, a);
     }
   }
   int flag = 0;
@@ -976,13 +1127,16 @@ void lp_begin(cphf_ctx* c, OzState& z, int s, const float* bra, int64_t nb) {
   // rows (j, a) over nu (W-gen A) and rows (nu, a) over j (T-gen A)
   z.braw.ensure((size_t)S2 * N * ldk * 2, c->counter());
   z.ebraw.ensure((size_t)N * 4, c->counter());
-  slice_rows_kernel<Split2, float><<<grid_warps(N, c->num_sms), 256, 0, c->stream>>>(
-      bra, N, nao, 0, nao, 0, 1, z.braw.as<__half>(), ldk, N * ldk, z.ebraw.as<int>());
-  z.brat.ensure((size_t)S2 * nao * nb * ldj * 2, c->counter());
-  z.ebrat.ensure((size_t)nao * nb * 4, c->counter());
-  slice_rows_kernel<Split2, float><<<grid_warps(nao * nb, c->num_sms), 256, 0, c->stream>>>(
-      bra, nao * nb, no, nao, 1, nao * no, nao, z.brat.as<__half>(), ldj, nao * nb * ldj, z.ebrat.as<int>());
-  count_launch(2);
+  {
+    ProfScope ps_slice(c, PROF_SLICE, 0.0, 8.0 * N * nao + 4.0 * N * ldk + 4.0 * nao * nb * ldj);
+    slice_rows_kernel<Split2, float><<<grid_warps(N, c->num_sms), 256, 0, c->stream>>>(
+        bra, N, nao, 0, nao, 0, 1, z.braw.as<__half>(), ldk, N * ldk, z.ebraw.as<int>());
+    z.brat.ensure((size_t)S2 * nao * nb * ldj * 2, c->counter());
+    z.ebrat.ensure((size_t)nao * nb * 4, c->counter());
+    slice_rows_kernel<Split2, float><<<grid_warps(nao * nb, c->num_sms), 256, 0, c->stream>>>(
+        bra, nao * nb, no, nao, 1, nao * no, nao, z.brat.as<__half>(), ldj, nao * nb * ldj, z.ebrat.as<int>());
+    count_launch(2);
+  }
   CPHF_CUDA(cudaGetLastError());
 }
 
@@ -1006,6 +1160,34 @@ void lp_tgen(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb
   ProfScope ps(c, PROF_TC_SPLIT, 2.0 * nao * nb * no * no * npc, 0.0);
   a.np = (int)npc;
   launch_batched<Split2>(c, mBt, mO, a);
+}
+
+void lp_tgen_planes(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, int64_t ldt, __half* hi,
+                    __half* lo, unsigned* mx, float* scale, float sA, float alpha, int* err) {
+  const int64_t nao = c->nao, naux = c->naux, no = c->spin[s].nocc, N = no * nb;
+  const int64_t ldj = z.spin[s].ldj;
+  constexpr int S2 = Split2::S;
+  const CUtensorMap mBt = make_map(z.brat.p, no, nao * nb, S2, ldj, BM, false);
+  const CUtensorMap mO = make_map(z.spin[s].O.p, no, no, S2 * naux, ldj, 64, false);
+  OzArgs a = base_args(z, (int)(nao * nb), (int)no);
+  a.err = err;
+  a.nkb = (int)div_up(no, BK);
+  a.a_depth = 1;
+  a.b_depth = (int)naux;
+  a.b_off = (int)P0;
+  a.e_row = z.ebrat.as<int>();
+  a.e_col = z.spin[s].eO.as<int>();
+  a.m_div = nao; a.s_m1 = 1; a.s_m2 = ldt * no; a.s_n = ldt; a.s_p = N * ldt;
+  a.np = (int)npc;
+  a.mx = mx;
+  a.tscale = scale;
+  a.out = hi;
+  a.out_lo = lo;
+  ProfScope ps(c, PROF_TC_SPLIT, 2.0 * 2.0 * nao * nb * no * no * npc, 2.0 * 2.0 * npc * N * nao);
+  CPHF_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned), c->stream));
+  launch_batched<Split2, EPI_MAX>(c, mBt, mO, a);
+  launch_t_scale(mx, sA, alpha, scale, c->stream);
+  launch_batched<Split2, EPI_SPLIT16>(c, mBt, mO, a);
 }
 
 void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, double alpha, float* out,
@@ -1038,14 +1220,17 @@ void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t
     a.np = (int)npc;
     launch_batched<Split2>(c, mBw, mZ, a);
   }
-  CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
-  colmax_rows_kernel<float><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.W.as<float>(), rows, N, ldj, no,
-                                                                                  z.mxc.as<unsigned long long>());
-  exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true, Split2::EOFF,
-                                                       z.e_col.as<int>(), z.colscale.as<double>());
-  slice_staging_kernel<Split2, float><<<grid_for(rows * no), 256, 0, c->stream>>>(
-      z.W.as<float>(), rows, N, ldj, no, z.e_col.as<int>(), z.Ws.as<__half>());
-  count_launch(3);
+  {
+    ProfScope ps_slice(c, PROF_SLICE, 0.0, (double)rows * (8.0 * no + 4.0 * ldj));
+    CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
+    colmax_rows_kernel<float><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.W.as<float>(), rows, N, ldj, no,
+                                                                                    z.mxc.as<unsigned long long>());
+    exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true, Split2::EOFF,
+                                                         z.e_col.as<int>(), z.colscale.as<double>());
+    slice_staging_kernel<Split2, float><<<grid_for(rows * no), 256, 0, c->stream>>>(
+        z.W.as<float>(), rows, N, ldj, no, z.e_col.as<int>(), z.Ws.as<__half>());
+    count_launch(3);
+  }
   {
     // term 2: out[mu, n] += alpha sum_{P, j} Z_P[mu, j] W_P[j, n]
     const CUtensorMap mZt = make_map(os.Zt.p, no, nao, S2 * naux, ldj, BM, false);
@@ -1063,7 +1248,7 @@ void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t
     a.colscale = z.colscale.as<double>();
     a.ld_out = nao;
     ProfScope ps(c, PROF_TC_SPLIT, 2.0 * nao * N * no * npc, 2.0 * S2 * no * npc * (nao + N));
-    launch_split<Split2, 128>(c, mZt, mW, a);
+    launch_split<Split2, 128>(c, z, mZt, mW, a);
   }
 }
 

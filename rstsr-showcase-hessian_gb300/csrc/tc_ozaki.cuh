@@ -3,6 +3,8 @@
 // (src/ri_jk/hess_r.rs:159-176), ~1e-10 relative to sum |A||B| per contraction, for the FP64
 // residual of the mixed-precision solve.
 #pragma once
+#include <cuda_fp16.h>
+
 #include <cstdint>
 
 #include "ctx.cuh"
@@ -26,6 +28,10 @@ void lp_begin(cphf_ctx* c, OzState& z, int s, const float* bra, int64_t nb);
 // T[Pl][(i,a)][nu] (FP32, row stride ldt) = sum_j bra[nu,j,a] O_P[j,i] for P in [P0, P0 + npc)
 void lp_tgen(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, float* T32, int64_t ldt,
              int* err);
+// the same T as FP16 hi / lo planes of s T (two passes: max |T| into *mx, launch_t_scale,
+// planes), hi and lo npc * nocc * nb * ldt apart in memory
+void lp_tgen_planes(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, int64_t ldt, __half* hi,
+                    __half* lo, unsigned* mx, float* scale, float sA, float alpha, int* err);
 // out (FP32 [nao, nocc_s, nb]) += alpha sum_{P in chunk} Z_P (Z_P^T bra)^T
 void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, double alpha, float* out,
                 int* err);

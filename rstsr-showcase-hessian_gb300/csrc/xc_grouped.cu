@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "ctx.cuh"
+#include "dfloat.cuh"
 #include "kernels.cuh"
 #include "xc_grouped.cuh"
 
@@ -32,25 +33,27 @@ struct XcCfg<float> {
 };
 
 // Register-tiled product over one K range; loadA(m, k) / loadB(k, n) return 0 outside.
-template <typename T, typename Cfg, typename LA_, typename LB_>
-__device__ __forceinline__ void tile_accumulate(T (&acc)[Cfg::TM][Cfg::TN], int64_t K, LA_ loadA, LB_ loadB,
-                                                T (*As)[Cfg::BM], T (*Bs)[Cfg::BN]) {
+// Operands are stored as T and converted to the compute type TC when staged (TC = dfloat:
+// FP64-accurate products on the FP32 pipes for the mixed solve's residual).
+template <typename TC, typename Cfg, typename LA_, typename LB_>
+__device__ __forceinline__ void tile_accumulate(TC (&acc)[Cfg::TM][Cfg::TN], int64_t K, LA_ loadA, LB_ loadB,
+                                                TC (*As)[Cfg::BM], TC (*Bs)[Cfg::BN]) {
   constexpr int BM = Cfg::BM, BN = Cfg::BN, BK = Cfg::BK, TM = Cfg::TM, TN = Cfg::TN;
   constexpr int NTX = BN / TN, NTY = BM / TM, NT = NTX * NTY;
   const int tid = threadIdx.x, tx = tid % NTX, ty = tid / NTX;
   for (int64_t k0 = 0; k0 < K; k0 += BK) {
     for (int e = tid; e < BM * BK; e += NT) {
       const int mm = e % BM, kk = e / BM;
-      As[kk][mm] = (k0 + kk < K) ? loadA(mm, k0 + kk) : (T)0;
+      As[kk][mm] = (k0 + kk < K) ? TC(loadA(mm, k0 + kk)) : TC(0);
     }
     for (int e = tid; e < BK * BN; e += NT) {
       const int kk = e % BK, nn = e / BK;
-      Bs[kk][nn] = (k0 + kk < K) ? loadB(k0 + kk, nn) : (T)0;
+      Bs[kk][nn] = (k0 + kk < K) ? TC(loadB(k0 + kk, nn)) : TC(0);
     }
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
-      T a[TM], b[TN];
+      TC a[TM], b[TN];
 #pragma unroll
       for (int i = 0; i < TM; ++i) a[i] = As[kk][ty + i * NTY];
 #pragma unroll
@@ -58,13 +61,13 @@ __device__ __forceinline__ void tile_accumulate(T (&acc)[Cfg::TM][Cfg::TN], int6
 #pragma unroll
       for (int i = 0; i < TM; ++i)
 #pragma unroll
-        for (int j = 0; j < TN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        for (int j = 0; j < TN; ++j) acc[i][j] = madd(a[i], b[j], acc[i][j]);
     }
     __syncthreads();
   }
 }
 
-template <typename T>
+template <typename T, typename TC>
 __global__ void __launch_bounds__(256) xc_gemm1_kernel(const XcGroupDev* __restrict__ groups, int ngroups,
                                                        const T* __restrict__ phi, const T* __restrict__ bra,
                                                        int64_t nao, int64_t N, int64_t pchunk, T* __restrict__ ket,
@@ -72,8 +75,8 @@ __global__ void __launch_bounds__(256) xc_gemm1_kernel(const XcGroupDev* __restr
   using Cfg = XcCfg<T>;
   constexpr int BM = Cfg::BM, BN = Cfg::BN, BK = Cfg::BK, TM = Cfg::TM, TN = Cfg::TN;
   constexpr int NTX = BN / TN, NTY = BM / TM;
-  __shared__ T As[BK][BM];
-  __shared__ T Bs[BK][BN];
+  __shared__ TC As[BK][BM];
+  __shared__ TC Bs[BK][BN];
   const int tid = threadIdx.x, tx = tid % NTX, ty = tid / NTX;
   for (int64_t w = blockIdx.x; w < total_tiles; w += gridDim.x) {
     int g = 0;
@@ -82,11 +85,11 @@ __global__ void __launch_bounds__(256) xc_gemm1_kernel(const XcGroupDev* __restr
     const int64_t local = w - G.tile_begin;
     const int64_t tm = local / tiles_n, tn = local % tiles_n;
     const int64_t m0 = tm * BM, n0 = tn * BN;
-    T acc[TM][TN];
+    TC acc[TM][TN];
 #pragma unroll
     for (int i = 0; i < TM; ++i)
 #pragma unroll
-      for (int j = 0; j < TN; ++j) acc[i][j] = (T)0;
+      for (int j = 0; j < TN; ++j) acc[i][j] = TC(0);
     const T* A = phi + G.phi_off;
     auto la = [&](int mm, int64_t k) -> T {
       const int64_t m = m0 + mm;
@@ -96,7 +99,7 @@ __global__ void __launch_bounds__(256) xc_gemm1_kernel(const XcGroupDev* __restr
       const int64_t n = n0 + nn;
       return n < N ? bra[G.lo + k + nao * n] : (T)0;
     };
-    tile_accumulate<T, Cfg>(acc, G.nwin, la, lb, As, Bs);
+    tile_accumulate<TC, Cfg>(acc, G.nwin, la, lb, As, Bs);
 #pragma unroll
     for (int i = 0; i < TM; ++i) {
       const int64_t m = m0 + ty + i * NTY;
@@ -104,13 +107,13 @@ __global__ void __launch_bounds__(256) xc_gemm1_kernel(const XcGroupDev* __restr
 #pragma unroll
       for (int j = 0; j < TN; ++j) {
         const int64_t n = n0 + tx + j * NTX;
-        if (n < N) ket[G.p_local + m + pchunk * n] = acc[i][j];
+        if (n < N) ket[G.p_local + m + pchunk * n] = static_cast<T>(acc[i][j]);
       }
     }
   }
 }
 
-template <typename T>
+template <typename T, typename TC>
 __global__ void __launch_bounds__(256) xc_gemm2_kernel(const XcGroupDev* __restrict__ groups, int ngroups,
                                                        const T* __restrict__ phi, const T* __restrict__ q,
                                                        int64_t nao, int64_t N, int64_t pchunk, T* __restrict__ out,
@@ -118,17 +121,17 @@ __global__ void __launch_bounds__(256) xc_gemm2_kernel(const XcGroupDev* __restr
   using Cfg = XcCfg<T>;
   constexpr int BM = Cfg::BM, BN = Cfg::BN, BK = Cfg::BK, TM = Cfg::TM, TN = Cfg::TN;
   constexpr int NTX = BN / TN, NTY = BM / TM;
-  __shared__ T As[BK][BM];
-  __shared__ T Bs[BK][BN];
+  __shared__ TC As[BK][BM];
+  __shared__ TC Bs[BK][BN];
   const int tid = threadIdx.x, tx = tid % NTX, ty = tid / NTX;
   for (int64_t w = blockIdx.x; w < tiles_m * tiles_n; w += gridDim.x) {
     const int64_t tm = w % tiles_m, tn = w / tiles_m;
     const int64_t m0 = tm * BM, n0 = tn * BN;
-    T acc[TM][TN];
+    TC acc[TM][TN];
 #pragma unroll
     for (int i = 0; i < TM; ++i)
 #pragma unroll
-      for (int j = 0; j < TN; ++j) acc[i][j] = (T)0;
+      for (int j = 0; j < TN; ++j) acc[i][j] = TC(0);
     for (int g = 0; g < ngroups; ++g) {
       const XcGroupDev G = groups[g];
       if (G.nwin == 0 || G.lo >= m0 + BM || G.lo + G.nwin <= m0) continue;  // window misses the tile
@@ -141,7 +144,7 @@ __global__ void __launch_bounds__(256) xc_gemm2_kernel(const XcGroupDev* __restr
         const int64_t n = n0 + nn;
         return n < N ? q[G.p_local + k + pchunk * n] : (T)0;
       };
-      tile_accumulate<T, Cfg>(acc, G.npts, la, lb, As, Bs);
+      tile_accumulate<TC, Cfg>(acc, G.npts, la, lb, As, Bs);
     }
 #pragma unroll
     for (int i = 0; i < TM; ++i) {
@@ -152,7 +155,7 @@ __global__ void __launch_bounds__(256) xc_gemm2_kernel(const XcGroupDev* __restr
         const int64_t n = n0 + tx + j * NTX;
         if (n >= N) continue;
         T* p = out + m + nao * n;
-        T v = (T)alpha * acc[i][j];
+        T v = (T)alpha * static_cast<T>(acc[i][j]);
         if (beta != 0.0) v = fma((T)beta, *p, v);
         *p = v;
       }
@@ -168,8 +171,17 @@ void xc_grouped_gemm1(cphf_ctx* c, const XcGroupDev* groups_dev, int ngroups, in
   using Cfg = XcCfg<T>;
   const int64_t tiles_n = div_up(N, Cfg::BN);
   const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(total_tiles, 8 * (int64_t)c->num_sms));
-  xc_gemm1_kernel<T><<<grid, 256, 0, c->stream>>>(groups_dev, ngroups, phi, bra, c->nao, N, pchunk, ket, total_tiles,
-                                                  tiles_n);
+  bool launched = false;
+  if constexpr (sizeof(T) == 8) {
+    if (c->f64_emulate) {
+      xc_gemm1_kernel<T, dfloat><<<grid, 256, 0, c->stream>>>(groups_dev, ngroups, phi, bra, c->nao, N, pchunk, ket,
+                                                              total_tiles, tiles_n);
+      launched = true;
+    }
+  }
+  if (!launched)
+    xc_gemm1_kernel<T, T><<<grid, 256, 0, c->stream>>>(groups_dev, ngroups, phi, bra, c->nao, N, pchunk, ket,
+                                                       total_tiles, tiles_n);
   count_launch();
   CPHF_CUDA(cudaGetLastError());
 }
@@ -180,8 +192,17 @@ void xc_grouped_gemm2(cphf_ctx* c, const XcGroupDev* groups_dev, int ngroups, co
   using Cfg = XcCfg<T>;
   const int64_t tiles_m = div_up(c->nao, Cfg::BM), tiles_n = div_up(N, Cfg::BN);
   const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(tiles_m * tiles_n, 8 * (int64_t)c->num_sms));
-  xc_gemm2_kernel<T><<<grid, 256, 0, c->stream>>>(groups_dev, ngroups, phi, q, c->nao, N, pchunk, out, alpha, beta,
-                                                  tiles_m, tiles_n);
+  bool launched = false;
+  if constexpr (sizeof(T) == 8) {
+    if (c->f64_emulate) {
+      xc_gemm2_kernel<T, dfloat><<<grid, 256, 0, c->stream>>>(groups_dev, ngroups, phi, q, c->nao, N, pchunk, out,
+                                                              alpha, beta, tiles_m, tiles_n);
+      launched = true;
+    }
+  }
+  if (!launched)
+    xc_gemm2_kernel<T, T><<<grid, 256, 0, c->stream>>>(groups_dev, ngroups, phi, q, c->nao, N, pchunk, out, alpha,
+                                                       beta, tiles_m, tiles_n);
   count_launch();
   CPHF_CUDA(cudaGetLastError());
 }
@@ -189,14 +210,19 @@ void xc_grouped_gemm2(cphf_ctx* c, const XcGroupDev* groups_dev, int ngroups, co
 int64_t xc_tiles_m(int64_t npts, bool f64) { return div_up(npts, f64 ? XcCfg<double>::BM : XcCfg<float>::BM); }
 int64_t xc_tiles_n(int64_t N, bool f64) { return div_up(N, f64 ? XcCfg<double>::BN : XcCfg<float>::BN); }
 
-// Chunks of consecutive batches whose intermediates (ket of every spin) fit the budget.
+// Chunks of consecutive batches whose intermediates (ket of every spin) fit the budget; one
+// cached plan per (precision, chunk cap, nb, nocc) so that the block widths of a Krylov solve
+// each keep theirs (captured operator graphs read the plan's device records).
 static XcPlan& xc_plan(cphf_ctx* c, size_t esize, int64_t nb) {
   const bool f64 = esize == 8;
-  XcPlan& pl = c->xc_plan[f64 ? 0 : 1];
   const int ns = c->nspin;
   const int64_t key[4] = {(int64_t)esize * 1000003 + c->cfg.xc_chunk_points, nb, c->spin[0].nocc,
                           ns > 1 ? c->spin[1].nocc : -1};
-  if (std::equal(key, key + 4, pl.key) && !pl.chunks.empty()) return pl;
+  for (auto& p : c->xc_plans)
+    if (std::equal(key, key + 4, p->key) && !p->chunks.empty()) return *p;
+  if (c->xc_plans.size() >= 64) c->xc_plans.erase(c->xc_plans.begin());  // frees its records
+  c->xc_plans.emplace_back(new XcPlan());
+  XcPlan& pl = *c->xc_plans.back();
   const int64_t budget = int64_t(8) << 30;  // bytes of ket intermediates per chunk
   int64_t per_point = 0;
   for (int s = 0; s < ns; ++s) per_point += c->spin[s].nocc * nb * (int64_t)esize;
@@ -255,6 +281,11 @@ void xc_response_grouped(cphf_ctx* c, const T* const* bra, int64_t nb, T* const*
   rho_buf.ensure((size_t)std::max<int64_t>(1, pl.max_pts * nb * 2) * sizeof(T), c->counter());
   const double fac = ns == 1 ? 4.0 : 2.0;  // hess_rks.rs:603, hess_uks.rs:438-439
   const XcGroupDev* gdev = pl.groups.as<XcGroupDev>();
+  double nnz = 0.0;  // stored AO values of the grid batches
+  for (const XcBatch& x : c->xc_batches) nnz += (double)x.npts * (double)x.nwin;
+  int64_t occ = 0;
+  for (int s = 0; s < ns; ++s) occ += c->spin[s].nocc;
+  ProfScope ps(c, sizeof(T) == 8 ? PROF_XC64 : PROF_XC32, 4.0 * nnz * occ * nb, 0.0);
   for (const XcChunk& ch : pl.chunks) {
     const int ng = (int)(ch.b1 - ch.b0);
     T* ket[2] = {ket_buf.as<T>(), ket_buf.as<T>() + ket_spin[0]};

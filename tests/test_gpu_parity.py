@@ -241,12 +241,12 @@ def _max_col_residual(c64, s, x):
     return float(np.linalg.norm(r, axis=0).max()), float(max(np.abs(a).max() for a in xs))
 
 
-@pytest.mark.parametrize("dims", [MEDIUM, TC_RAGGED, MEDIUM_U])
+@pytest.mark.parametrize("dims", [MEDIUM, TC_RAGGED, MEDIUM_U, GRID_R])
 @pytest.mark.parametrize("mode", [1, 2])
 def test_emulated_fp64_residual(dims, mode):
     """The residual of the mixed solve's first correction, computed with the emulated FP64
-    operator (mode 1: double-float GEMMs; mode 2: plus the K term on the tensor cores with
-    exact BF16 slices, chunked over aux functions), matches the native FP64 residual of the
+    operator (mode 1: double-float GEMMs, XC included; mode 2: plus the K term on the tensor
+    cores with exact BF16 slices, chunked over aux functions), matches the native FP64 residual of the
     same x to 1e-9 relative to max |x| (the split-FP16 operator of the inner solves is ~1e-6)."""
     s = synth.make_system(dims, seed=15)
     rhs = s.rhs[0] if s.nspin == 1 else s.rhs
@@ -285,6 +285,22 @@ def test_mixed_precision_solve(dims, dfloat):
         m1, me = ctx.finalize_cphf(f1, s1, x[0] if s.nspin == 1 else x)
         h.append(ctx.get_cphf_hess(f1, s1, m1, me))
     assert np.abs(h[0] - h[1]).max() < 1e-7
+
+
+@pytest.mark.parametrize("dims", [MEDIUM, GRID_U])
+def test_mixed_solve_cuda_graphs(dims):
+    """Inner operator replayed from captured CUDA graphs (one per block width, two solves so
+    the second replays every width) gives the eager operator's solution."""
+    s = synth.make_system(dims, seed=17)
+    rhs = s.rhs[0] if s.nspin == 1 else s.rhs
+    eager = make_ctx(s, precision="mixed", cuda_graphs=0)
+    graph = make_ctx(s, precision="mixed", cuda_graphs=1)
+    x0 = eager.solve_dimless_cphf(rhs)
+    for _ in range(2):
+        x1 = graph.solve_dimless_cphf(rhs)
+        assert graph.last_stats["residual_max"] < 1e-8
+        for a, b in zip([x1] if s.nspin == 1 else x1, [x0] if s.nspin == 1 else x0):
+            assert np.abs(a - b).max() < 1e-9
 
 
 def test_gpu_krylov_reference_fixture():
