@@ -52,6 +52,10 @@ def parse():
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison solve")
     p.add_argument("--cpu-sample", type=int, default=12, help="RHS columns of the CPU baseline sample")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg (profiling runs)")
+    p.add_argument("--inner-tol", type=float, default=None, help="Krylov tol of the inner solves (library default)")
+    p.add_argument("--no-graphs", action="store_true", help="run the inner operator eagerly (no CUDA graphs)")
+    p.add_argument("--verify-cols", type=int, default=0,
+                   help="verify the FP64 residual on the first K perturbations only (0: all)")
     p.add_argument("--no-learned", action="store_true", help="do not use the trained initial guess")
     p.add_argument("--fp64-tol", type=float, default=1e-10, help="Krylov tol of the plain FP64 solve")
     p.add_argument("--fp64-lindep", type=float, default=1e-20,
@@ -92,19 +96,34 @@ def max_over_ranks(world, v):
 
 
 # ---------------------------------------------------------------- CPU (oracle) timing
+def cpu_oracle_driver(s):
+    """The reference algorithm restated on the CPU (oracle): RHF/UHF driver with the RI-JK and,
+    for RKS/UKS workloads, the XC response plugins."""
+    from oracle import cphf as ocphf
+    from oracle import rijk as orijk
+    from oracle import xc as oxc
+    mocc = [s.mo_coeff[t][:, :s.nocc[t]] for t in range(s.nspin)]
+    g = s.grid
+    if s.nspin == 1:
+        plugs = [lambda b: orijk.rhf_response_bra(s.cderi, s.mo_coeff[0], s.mo_occ[0], b, s.scale_j, s.scale_k)]
+        if g is not None:
+            plugs.append(lambda b: oxc.rks_response_bra(g.ao, g.weights, g.fxc, b, mocc[0]))
+        return ocphf.RHF(s.mo_coeff[0], s.mo_occ[0], s.mo_energy[0], plugs, s.natm)
+    plugs = [lambda b: orijk.uhf_response_bra(s.cderi, s.mo_coeff, s.mo_occ, b, s.scale_j, s.scale_k)]
+    if g is not None:
+        plugs.append(lambda b: oxc.uks_response_bra(g.ao, g.weights, g.fxc, b, mocc))
+    return ocphf.UHF(s.mo_coeff, s.mo_occ, s.mo_energy, plugs, s.natm)
+
+
 def cpu_oracle_estimate(s, ncols):
     """Reference algorithm on the host (oracle port): a real Krylov solve of `ncols` RHS
     columns with the full-size operator gives the operator-call count; single matvecs at
     ncols and 2*ncols give the per-call cost model t0 + t1*nb, extrapolated to all columns."""
-    from oracle import cphf as ocphf
-    from oracle import rijk as orijk
-    C, occ, e = s.mo_coeff[0], s.mo_occ[0], s.mo_energy[0]
-    plug = lambda bra: orijk.rhf_response_bra(s.cderi, C, occ, bra, s.scale_j, s.scale_k)  # noqa: E731
-    drv = ocphf.RHF(C, occ, e, [plug], s.natm)
+    drv = cpu_oracle_driver(s)
     nrhs = s.rhs[0].shape[2] * s.rhs[0].shape[3]
-    rhs = s.rhs[0].reshape(s.nao, s.nocc[0], nrhs, order="F")
-    x1 = rhs[:, :, :ncols]
-    x2 = rhs[:, :, :2 * ncols]
+    rhs = [r.reshape(s.nao, s.nocc[t], nrhs, order="F") for t, r in enumerate(s.rhs[:s.nspin])]
+    cut = (lambda k: rhs[0][:, :, :k]) if s.nspin == 1 else (lambda k: [r[:, :, :k] for r in rhs])
+    x1, x2 = cut(ncols), cut(2 * ncols)
     t = time.perf_counter(); drv.response_dimless_cphf(x1); t1 = time.perf_counter() - t
     t = time.perf_counter(); drv.response_dimless_cphf(x2); t2 = time.perf_counter() - t
     slope = max((t2 - t1) / ncols, 1e-12)
@@ -243,8 +262,9 @@ def run_gpu(args, world, rank, local):
 
     weights = ROOT / "rstsr-showcase-hessian_gb300" / "cphf_gb300" / "mlp_weights.npy"
     learned = weights.exists() and not args.no_learned and nspin == 1
+    inner = {} if args.inner_tol is None else dict(inner_tol=args.inner_tol)
     mixed = make_ctx("mixed", verify_residual=0, use_learned_guess=1 if learned else 0,
-                     residual_dfloat=args.residual)
+                     residual_dfloat=args.residual, cuda_graphs=0 if args.no_graphs else 1, **inner)
     if learned:
         mixed.set_mlp_weights(np.load(weights))
     # device-resident inputs and outputs (F-contiguous views of C-ordered tensors)
@@ -260,7 +280,6 @@ def run_gpu(args, world, rank, local):
     clocks.start()
     barrier(world)
     torch.cuda.synchronize()
-    mixed.profile(True)
     l0 = mixed.kernel_launches
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
@@ -272,11 +291,21 @@ def run_gpu(args, world, rank, local):
     torch.cuda.synchronize()
     barrier(world)
     launches = mixed.kernel_launches - l0
-    prof = mixed.profile_report()
-    mixed.profile(False)
     clk = clocks.stop()
     t_step = ev0.elapsed_time(ev1) * 1e-3 / args.steps
     t_step = max_over_ranks(world, t_step)
+
+    # per-kernel-class breakdown: one more solve with the CUDA-event profiler on (which runs the
+    # operator eagerly instead of replaying its graphs), outside the timed region
+    mixed.profile(True)
+    ep0, ep1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ep0.record(stream)
+    mixed.solve_dimless_cphf(arg(rhs_d), out=arg(out_d))
+    ep1.record(stream)
+    torch.cuda.synchronize()
+    t_prof = ep0.elapsed_time(ep1) * 1e-3
+    prof = mixed.profile_report()
+    mixed.profile(False)
 
     # end to end through the C ABI with pinned host buffers (copies inside the timed region)
     rhs_p = [torch.from_numpy(np.ascontiguousarray(r.transpose(3, 2, 1, 0))).pin_memory() for r in rhs_h]
@@ -290,6 +319,10 @@ def run_gpu(args, world, rank, local):
         mixed.solve_dimless_cphf(arg(rhs_pf), out=arg(out_pf))
     t_e2e = max_over_ranks(world, (time.perf_counter() - t) / args.steps)
     x_mixed = [o.numpy().transpose(3, 2, 1, 0).copy(order="F") for o in out_p]
+    tc_active = mixed.tensor_cores_active
+    mixed.close()  # release its device memory before the FP64 context is built
+    del rhs_d, out_d
+    torch.cuda.empty_cache()
 
     # plain FP64 solve of the same system (the reference's arithmetic), timed once
     fp64 = make_ctx("fp64", cphf_tol=args.fp64_tol, cphf_lindep=args.fp64_lindep)
@@ -301,14 +334,23 @@ def run_gpu(args, world, rank, local):
         st64 = fp64.last_stats
         x64 = x64 if nspin == 2 else [x64]
 
-    # verification outside the timed regions: FP64 residuals and Hessian blocks
+    # verification outside the timed regions: FP64 residuals (on the first --verify-cols
+    # perturbations, all by default) and Hessian blocks
+    ncols_v = args.verify_cols if args.verify_cols > 0 else None
+    t_verify = [0.0]
+
     def residual(x):
-        y = fp64.response_dimless_cphf(arg(x))
+        bs = [b.reshape(b.shape[0], b.shape[1], -1, order="F")[:, :, :ncols_v] for b in rhs_h]
+        xs = [xx.reshape(xx.shape[0], xx.shape[1], -1, order="F")[:, :, :ncols_v] for xx in x]
+        t = time.perf_counter()
+        y = fp64.response_dimless_cphf(arg([np.asfortranarray(v) for v in xs]))
+        t_verify[0] = time.perf_counter() - t
         y = y if nspin == 2 else [y]
-        return max(float(np.linalg.norm((b - xx - yy).reshape(-1, b.shape[2] * b.shape[3], order="F"),
-                                        axis=0).max()) for b, xx, yy in zip(rhs_h, x, y))
+        return max(float(np.linalg.norm((b - xx - yy).reshape(-1, b.shape[2], order="F"), axis=0).max())
+                   for b, xx, yy in zip(bs, xs, y))
 
     res_mixed = residual(x_mixed)
+    t_verify_mixed = t_verify[0]
     hess_diff = None
     if not args.no_fp64:
         fp64_res = residual(x64)
@@ -328,7 +370,11 @@ def run_gpu(args, world, rank, local):
         "tw_term2_tcgen05_f16x3": "FP16 hi/lo, the tensor pipe executes 3 split products",
         "kterm_tcgen05_bf16x6_exact": "exact BF16 slices, the tensor pipe executes 21 slice products",
     }
-    if dom_name == "gemm_fp64_simt":
+    if dom_name == "slice_scale_split":
+        roof = dict(bound="hbm", achieved=dom["bytes"] / dom["ms"] / 1e6, peak=hbm, unit="GB/s",
+                    peak_source=f"{peak_src} HBM copy; achieved counts the algorithmic bytes (operands read, "
+                                "slice planes written) of the slicing / scaling kernels")
+    elif dom_name == "gemm_fp64_simt":
         peak = measure_fp64_peak()
         roof = dict(bound="tensor", achieved=dom["flops"] / dom["ms"] / 1e9, peak=peak, unit="TFLOP/s",
                     peak_source="in-run cuBLAS FP64 GEMM 8192^3 (FP64 has no entry in MEASURED_PEAKS.json)")
@@ -343,12 +389,15 @@ def run_gpu(args, world, rank, local):
     traffic = None
     if dom_name in traffic_ratio and dom.get("bytes", 0) > 0:
         traffic = traffic_ratio[dom_name] * dom["bytes"] / dom["launches"]
-    roof.update(kernel=dom_name, frac=roof["achieved"] / roof["peak"], traffic=traffic,
+    if dom_name.startswith("xc_grouped"):
+        roof.update(bound="fp64 pipe" if dom_name.endswith("fp64") else "fp32 pipe", peak=None,
+                    peak_source="SIMT GEMM (no tensor-core form); see the per-class TFLOP/s")
+    roof.update(kernel=dom_name, frac=roof["achieved"] / roof["peak"] if roof.get("peak") else None, traffic=traffic,
                 traffic_unit="bytes per launch" if traffic else None,
                 launches=dom["launches"], avg_launch_ms=dom["ms"] / dom["launches"],
-                share_of_step=dom["ms"] * 1e-3 / (t_step * args.steps))
+                share_of_step=dom["ms"] * 1e-3 / t_prof)
 
-    cpu = cpu_oracle_estimate(s, args.cpu_sample) if rank == 0 and nspin == 1 and not args.no_cpu else None
+    cpu = cpu_oracle_estimate(s, args.cpu_sample) if rank == 0 and not args.no_cpu else None
     st = stats[-1]
     line = dict(
         metric=METRIC, value=t_step, unit="s", n_gpus=args.gpus, steps=args.steps, warmup=args.warmup,
@@ -359,19 +408,27 @@ def run_gpu(args, world, rank, local):
         data=f"synthetic (seeded generator, {args.workload}, seed {args.seed})",
         config=dict(workload=args.workload, description=WORKLOAD_DESC.get(args.workload, args.workload),
                     precision="mixed", learned_guess=learned, residual_mode=args.residual,
+                    inner_tol=args.inner_tol if args.inner_tol is not None else 1e-6,
+                    cuda_graphs=not args.no_graphs,
                     parallelism="replicas" if world > 1 else "single GPU",
                     l2="inputs larger than L2 (dense cderi FP64 %.1f GB)" % (s.nao ** 2 * s.naux * 8 / 1e9)),
         fp64_plain=None if args.no_fp64 else dict(value=t_fp64, unit="s", aop_calls=st64["aop_calls"],
                                                   cycles=st64["cycles"], tol=args.fp64_tol,
                                                   lindep=args.fp64_lindep),
         speedup_vs_fp64_plain=None if args.no_fp64 else t_fp64 / t_step,
-        residual=dict(mixed_verified=res_mixed, fp64_plain_verified=fp64_res, target=1e-8),
+        residual=dict(mixed_verified=res_mixed, fp64_plain_verified=fp64_res, target=1e-8,
+                      verified_columns=ncols_v or int(np.prod(rhs_h[0].shape[2:])),
+                      fp64_operator_s=t_verify_mixed),
         hessian_max_abs_diff_vs_fp64=hess_diff,
         solve_stats=dict(refine_steps=st["refine_steps"], fp64_matvec_columns=st["fp64_matvec_columns"],
                          lowp_matvec_columns=st["lowp_matvec_columns"], cycles=st["cycles"],
-                         tensor_cores=mixed.tensor_cores_active),
-        kernel_classes={k: dict(launches=v["launches"], ms=round(v["ms"], 3),
-                                tflops=round(v["flops"] / max(v["ms"], 1e-9) / 1e9, 2)) for k, v in prof.items()},
+                         tensor_cores=tc_active),
+        kernel_classes=dict(
+            note="one profiled solve (eager operator, CUDA events per class) outside the timed region",
+            solve_s=t_prof,
+            **{k: dict(launches=v["launches"], ms=round(v["ms"], 3),
+                       tflops=round(v["flops"] / max(v["ms"], 1e-9) / 1e9, 2),
+                       gbs=round(v["bytes"] / max(v["ms"], 1e-9) / 1e6, 1)) for k, v in prof.items()}),
         e2e=dict(value=t_e2e, unit="s", h2d_bytes_per_step=h2d, d2h_bytes_per_step=d2h),
         gpu_launches=int(launches),
         roofline=roof,

@@ -377,7 +377,15 @@ bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, d
       launch_axpby(1.0 / scale, x0, 0.0, adl, n * nset, s);  // initial guess in scaled units
       g0 = adl;
     }
-    krylov_device(c, op, rr, g0, n, nset, p, dlt, st);
+    // the inner solve's Gram / projection GEMMs in double-float (its operator is ~1e-6 accurate)
+    c->f64_emulate = c->cfg.residual_dfloat != 0;
+    try {
+      krylov_device(c, op, rr, g0, n, nset, p, dlt, st);
+    } catch (...) {
+      c->f64_emulate = false;
+      throw;
+    }
+    c->f64_emulate = false;
     launch_axpby(scale, dlt, 0.0, dlt, n * nset, s);
     launch_axpby(1.0, dlt, 1.0, x, n * nset, s);
     st->refine_steps += 1;
