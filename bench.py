@@ -367,7 +367,9 @@ def run_gpu(args, world, rank, local):
     dom_name, dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
     tensor_notes = {
         "kterm_tcgen05_f16x3": "FP16 hi/lo, the tensor pipe executes 3 split products",
-        "tw_term2_tcgen05_f16x3": "FP16 hi/lo, the tensor pipe executes 3 split products",
+        "tgen_tcgen05_f16x3": "FP16 hi/lo, the tensor pipe executes 3 split products (twice: max, then planes)",
+        "wgen_tcgen05_f16x3": "FP16 hi/lo, the tensor pipe executes 3 split products",
+        "term2_tcgen05_f16x3": "FP16 hi/lo, the tensor pipe executes 3 split products",
         "kterm_tcgen05_bf16x6_exact": "exact BF16 slices, the tensor pipe executes 21 slice products",
     }
     if dom_name == "slice_scale_split":

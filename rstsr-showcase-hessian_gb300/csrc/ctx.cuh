@@ -20,6 +20,7 @@ struct OzSpin {
   DevBuf O, eO;        // [6][naux][nocc(i)][ldj] of O_P[j, i], K = j; exponent per (P, i)
   DevBuf Z, eZ;        // [6][naux][nocc(i)][ldk] of Z_P[nu, i], K = nu; exponent per (P, i)
   DevBuf Zt, sZt, eZt; // [6][naux][nao(mu)][ldj] of Z_P[mu, j], K = j; scale per mu over (j, P)
+  DevBuf Omax;         // split FP16: max |O_P| per aux function (float bits), for the T bound
   int64_t ldj = 0;     // padded K = nocc rows
   bool ready = false;
 };
@@ -28,7 +29,7 @@ struct OzState {
   DevBuf rowscale, e_row, mx;  // per-row power-of-two scales of A
   OzSpin spin[2];
   // per-call scratch: bra slices (both K orders), T / Wt staging (FP32 pairs) and slices
-  DevBuf braw, ebraw, brat, ebrat, T, B, W, Ws;
+  DevBuf braw, ebraw, brat, ebrat, T, B, W, Ws, braS;
   DevBuf colscale, e_col, mxc, err, tune_out;
   int64_t ldk = 0;
   bool ready = false;
@@ -146,7 +147,9 @@ enum ProfClass {
   PROF_KRYLOV = 7,
   PROF_XC64 = 8,
   PROF_XC32 = 9,
-  PROF_NCLASS = 10
+  PROF_TC_WGEN = 10,
+  PROF_TC_TERM2 = 11,
+  PROF_NCLASS = 12
 };
 extern const char* const kProfNames[PROF_NCLASS];
 

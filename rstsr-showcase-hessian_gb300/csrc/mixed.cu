@@ -120,8 +120,8 @@ static void rijk_response_lowp(cphf_ctx* c, float* const* bra, int64_t nb, float
         // T-generation kernel, then W-generation and term 2 per chunk
         int* err = L.err.as<int>();
         lp_begin(c, L.lp, s, bra[s], nb);
-        tc_k_term1(c, L.Bhi, L.Blo, L.ldk, sp.O32.as<float>(), bra[s], no, nb, -c->scale_k, out[s], L.s_Thi,
-                   L.s_Tlo, [&](int64_t P0, int64_t npc, __half* hi, __half* lo, unsigned* mx, float* scale) {
+        tc_k_term1(c, L.Bhi, L.Blo, L.ldk, no, nb, out[s], L.s_Thi, L.s_Tlo,
+                   [&](int64_t P0, int64_t npc, __half* hi, __half* lo, unsigned* mx, float* scale) {
                      lp_tgen_planes(c, L.lp, s, P0, npc, nb, L.ldk, hi, lo, mx, scale, (float)L.sA,
                                     (float)-c->scale_k, err);
                    });

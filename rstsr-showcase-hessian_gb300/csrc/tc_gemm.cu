@@ -12,7 +12,7 @@
 //
 // Kernel structure (one CTA per SM, 4 warps):
 //   warp 0 lane 0  -- TMA producer: 3-D tiled loads (K = nu, row = mu or n, P) of the four
-//                     planes into a 2-stage ring of 128B-swizzled shared-memory tiles;
+//                     planes into a 2-stage ring of 128B-swizzled shared-memory tiles (K = 64);
 //   warp 1 lane 0  -- MMA issuer: tcgen05.mma.cta_group::1.kind::f16 (M=128, N=256, K=16),
 //                     tcgen05.commit frees a stage when its MMAs retire;
 //   warp 2         -- TMEM allocation (256 FP32 columns) and release;
@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(128, 1)
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 8);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES), accum = smem_u32(bars + 2 * STAGES);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -191,25 +191,6 @@ __global__ void split_cderi_kernel(const double* __restrict__ Bd, int64_t nao, i
   }
 }
 
-// |x| maxima: one atomicMax on the float bit pattern per warp.
-// max |x| over rows [0, rows) of length `valid` with row stride `ld` (ld % 4 == 0: rows start
-// 16-byte aligned; float4 loads, scalar tail)
-__global__ void absmax_f32_kernel(const float* __restrict__ x, int64_t rows, int64_t ld, int64_t valid,
-                                  unsigned* out) {
-  float m = 0.f;
-  const int64_t v4 = valid / 4;
-  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
-    const float4* row4 = reinterpret_cast<const float4*>(x + r * ld);
-    for (int64_t v = threadIdx.x; v < v4; v += blockDim.x) {
-      const float4 q = row4[v];
-      m = fmaxf(m, fmaxf(fmaxf(fabsf(q.x), fabsf(q.y)), fmaxf(fabsf(q.z), fabsf(q.w))));
-    }
-    for (int64_t v = 4 * v4 + threadIdx.x; v < valid; v += blockDim.x) m = fmaxf(m, fabsf(x[r * ld + v]));
-  }
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
-}
-
 __global__ void absmax_f64_kernel(const double* __restrict__ x, int64_t n, unsigned* out) {
   float m = 0.f;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
@@ -232,22 +213,6 @@ __global__ void t_scale_kernel(const unsigned* mx, float sA, float alpha, float*
   scale[1] = alpha / (sA * s);
 }
 
-// T32 chunk [np][N][ldk] (FP32) -> planes, four elements per thread (n % 4 == 0); nu >= nao
-// is split too but never read (outside the TMA extent)
-__global__ void split_t_kernel(const float4* __restrict__ t32, int64_t n4, const float* __restrict__ scale,
-                               uint2* __restrict__ hi, uint2* __restrict__ lo) {
-  const float s = scale[0];
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n4; t += (int64_t)gridDim.x * blockDim.x) {
-    float4 x = t32[t];
-    x.x *= s; x.y *= s; x.z *= s; x.w *= s;
-    const __half2 h01 = __floats2half2_rn(x.x, x.y), h23 = __floats2half2_rn(x.z, x.w);
-    const float2 f01 = __half22float2(h01), f23 = __half22float2(h23);
-    const __half2 l01 = __floats2half2_rn(x.x - f01.x, x.y - f01.y), l23 = __floats2half2_rn(x.z - f23.x, x.w - f23.y);
-    hi[t] = make_uint2(*reinterpret_cast<const unsigned*>(&h01), *reinterpret_cast<const unsigned*>(&h23));
-    lo[t] = make_uint2(*reinterpret_cast<const unsigned*>(&l01), *reinterpret_cast<const unsigned*>(&l23));
-  }
-}
-
 // ---- host side ---------------------------------------------------------------------------
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -264,7 +229,8 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
-// 3-D FP16 tensor map: dims {K (= nao), rows, planes}, row stride ldk elements, 128B swizzle.
+// 3-D FP16 tensor map: dims {K (= nao), rows, planes}, row stride ldk elements, box {64, rows, 1},
+// 128B swizzle.
 CUtensorMap make_map(const void* base, int64_t K, int64_t rows, int64_t depth, int64_t ldk, int box_rows) {
   CUtensorMap m;
   std::memset(&m, 0, sizeof(m));
@@ -333,8 +299,8 @@ void tc_prepare_cderi(cphf_ctx* c, DevBuf& hi, DevBuf& lo, int64_t& ldk) {
   CPHF_CUDA(cudaGetLastError());
 }
 
-void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, const float* O32, const float* bra,
-                int64_t no, int64_t nb, double alpha, float* out, DevBuf& Thi, DevBuf& Tlo, const TPlanes& tplanes) {
+void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, int64_t no, int64_t nb,
+                float* out, DevBuf& Thi, DevBuf& Tlo, const TPlanes& tplanes) {
   LowpState& L = *c->lowp;
   const int64_t nao = c->nao, naux = c->naux;
   const int64_t N = no * nb;
@@ -345,11 +311,9 @@ void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, 
   const size_t plane = (size_t)np * N * ldk * 2;
   Thi.ensure(plane, c->counter());
   Tlo.ensure(plane, c->counter());
-  // T32 staging (only without the fused plane generator) + scale scratch
-  const size_t t32 = tplanes ? 0 : (size_t)np * N * ldk;
-  L.s_acc.ensure(t32 * 4 + 64, c->counter());
-  float* T32 = L.s_acc.as<float>();
-  unsigned* mx = reinterpret_cast<unsigned*>(T32 + t32);
+  // scale scratch: max |T| (float bits) and the two scale factors
+  L.s_acc.ensure(64, c->counter());
+  unsigned* mx = L.s_acc.as<unsigned>();
   float* scale = reinterpret_cast<float*>(mx + 4);
   L.err.ensure(sizeof(int), c->counter());
   const int m_tiles = (int)div_up(nao, BM), n_tiles = (int)div_up(N, BN);
@@ -357,28 +321,9 @@ void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, 
   const int ppc = 16;
   for (int64_t P0 = 0; P0 < naux; P0 += np) {
     const int64_t npc = std::min<int64_t>(np, naux - P0);
-    // T32[Pl][(i,a)][nu] = sum_j bra[nu, j, a] O_P[j, i]: one tall GEMM per aux function,
-    // rows (nu, a) (two-level index), columns i, K = j
-    if (tplanes) {
-      // FP16 planes of T and their scale straight from the T generator (no FP32 T in HBM)
-      tplanes(P0, npc, Thi.as<__half>(), Tlo.as<__half>(), mx, scale);
-    } else {
-      GemmDesc t;
-      t.M = nao * nb; t.N = no; t.K = no; t.batch1 = npc;
-      t.A = bra; t.a_m = 1; t.m_div = nao; t.a_m2 = nao * no; t.a_k = nao; t.a_b1 = 0;
-      t.B = O32 + P0 * no * no; t.b_k = 1; t.b_n = no; t.b_b1 = no * no;
-      t.C = T32; t.c_m = 1; t.c_m2 = ldk * no; t.c_n = ldk; t.c_b1 = N * ldk;
-      gemm32(c, t);
-      const int64_t tn = npc * N * ldk;
-      ProfScope ps_slice(c, PROF_SLICE, 0.0, 4.0 * npc * N * nao + 12.0 * tn);
-      CPHF_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned), c->stream));
-      absmax_f32_kernel<<<(unsigned)std::min<int64_t>(npc * N, 8 * (int64_t)c->num_sms), 256, 0, c->stream>>>(
-          T32, npc * N, ldk, nao, mx);
-      t_scale_kernel<<<1, 1, 0, c->stream>>>(mx, (float)L.sA, (float)alpha, scale);
-      split_t_kernel<<<grid_for(tn / 4), 256, 0, c->stream>>>(reinterpret_cast<const float4*>(T32), tn / 4, scale,
-                                                              Thi.as<uint2>(), Tlo.as<uint2>());
-      count_launch(3);
-    }
+    // FP16 planes of T_P[nu, (i,a)] = sum_j bra[nu, j, a] O_P[j, i] and their scale from the
+    // T generator (no FP32 T in HBM)
+    tplanes(P0, npc, Thi.as<__half>(), Tlo.as<__half>(), mx, scale);
     const CUtensorMap mAh = make_map(Bhi.p, nao, nao, naux, ldk, BM);
     const CUtensorMap mAl = make_map(Blo.p, nao, nao, naux, ldk, BM);
     const CUtensorMap mBh = make_map(Thi.p, nao, N, npc, ldk, BN);

@@ -21,11 +21,10 @@ void tc_prepare_cderi(cphf_ctx* c, DevBuf& hi, DevBuf& lo, int64_t& ldk);
 // bits) and scale[0] = s, scale[1] = alpha / (sA s) as launch_t_scale writes them
 using TPlanes =
     std::function<void(int64_t P0, int64_t npc, __half* hi, __half* lo, unsigned* mx, float* scale)>;
-// out (FP32 [nao, nocc, nb]) += alpha * sum_P B_P bra O_P; bra FP32 [nao, nocc, nb], O32 [nocc, nocc, naux];
-// T comes from `tplanes` when given, else from an FP32 CUDA-core GEMM, a max and a split
-void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, const float* O32,
-                const float* bra, int64_t nocc, int64_t nb, double alpha, float* out, DevBuf& Thi,
-                DevBuf& Tlo, const TPlanes& tplanes = TPlanes());
+// out (FP32 [nao, nocc, nb]) += alpha * sum_P B_P T_P with T_P's FP16 planes and scale from
+// `tplanes` (alpha enters through scale[1])
+void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, int64_t nocc, int64_t nb,
+                float* out, DevBuf& Thi, DevBuf& Tlo, const TPlanes& tplanes);
 // scale[0] = 2^(14 - e) for max |T| = *mx < 2^e, scale[1] = alpha / (sA scale[0])
 void launch_t_scale(const unsigned* mx, float sA, float alpha, float* scale, cudaStream_t stream);
 

@@ -99,9 +99,8 @@ struct OzArgs {
   int a_per_p;              // A depth advances with the aux function
   int np, p_per_cta;        // batched: aux functions of the launch, per CTA
   int kb_per_cta;           // split: K blocks per CTA (<= KMAX / BK, the exactness bound)
-  // batched split-FP16 T generation fused with the FP16 split of T (tc_gemm.cu's term 1):
-  // pass 1 takes max |T| into *mx (float bits), pass 2 writes hi / lo planes of T * (*tscale)
-  unsigned* mx;
+  // batched split-FP16 T generation writing the FP16 hi / lo planes of T * (*tscale) for
+  // tc_gemm.cu's term 1
   const float* tscale;
   void* out_lo;             // the lo plane (same layout as out, the hi plane)
   // split mode epilogue: out [m + ld_out n] += value rowscale[m] colscale[n] (double: Exact6, float: Split2)
@@ -298,8 +297,8 @@ __device__ __forceinline__ float pow2f(int e) {
   return (e >= -126 && e <= 127) ? __int_as_float((e + 127) << 23) : ldexpf(1.f, e);
 }
 
-// EPI: 0 store the scaled values (T / W staging), 1 max |value| only, 2 FP16 hi / lo planes
-enum { EPI_STORE = 0, EPI_MAX = 1, EPI_SPLIT16 = 2 };
+// EPI: store the scaled values (T / W staging) or FP16 hi / lo planes of them times *tscale
+enum { EPI_STORE = 0, EPI_SPLIT16 = 2 };
 
 template <class PR, int BN, int EPI = EPI_STORE>
 __global__ void __launch_bounds__(320, PR::S == 6 ? 1 : 2)
@@ -452,7 +451,6 @@ __global__ void __launch_bounds__(320, PR::S == 6 ? 1 : 2)
         } else {
           float v[32];
           tmem_ld32(lane_base + (uint32_t)(c * 32), v);
-          float mx = 0.f;
           const float ts = EPI == EPI_SPLIT16 ? *args.tscale : 1.f;
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
@@ -461,8 +459,6 @@ __global__ void __launch_bounds__(320, PR::S == 6 ? 1 : 2)
             if (row_ok && n < args.N) {
               if constexpr (EPI == EPI_STORE) {
                 reinterpret_cast<float*>(args.out)[pbase + n * args.s_n] = v[j] * f;
-              } else if constexpr (EPI == EPI_MAX) {
-                mx = fmaxf(mx, fabsf(v[j] * f));
               } else {
                 const float x = (v[j] * f) * ts;
                 const __half h = __float2half_rn(x);
@@ -471,10 +467,6 @@ __global__ void __launch_bounds__(320, PR::S == 6 ? 1 : 2)
                 reinterpret_cast<__half*>(args.out_lo)[off] = __float2half_rn(x - __half2float(h));
               }
             }
-          }
-          if constexpr (EPI == EPI_MAX) {
-            for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-            if (lane == 0) atomicMax(args.mx, __float_as_uint(mx));
           }
         }
         fence_before_sync();
@@ -683,6 +675,52 @@ __global__ void slice_staging_kernel(const TIn* __restrict__ T, int64_t rows, in
   }
 }
 
+// max_{j,i} |O_P[j, i]| per aux function P (float bits); one block per P
+__global__ void omax_kernel(const float* __restrict__ O, int64_t no2, int64_t naux, unsigned* __restrict__ omax) {
+  __shared__ float red[32];
+  for (int64_t P = blockIdx.x; P < naux; P += gridDim.x) {
+    float m = 0.f;
+    for (int64_t t = threadIdx.x; t < no2; t += blockDim.x) m = fmaxf(m, fabsf(O[P * no2 + t]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
+      omax[P] = __float_as_uint(m);
+    }
+    __syncthreads();
+  }
+}
+
+// max over (nu, a) of sum_j |bra[nu + nao j + nao no a]| (float bits, atomicMax into *out)
+__global__ void bra_rowsum_max_kernel(const float* __restrict__ bra, int64_t nao, int64_t no, int64_t nb,
+                                      unsigned* __restrict__ out) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;  // nu + nao a
+  float sum = 0.f;
+  if (r < nao * nb) {
+    const int64_t nu = r % nao, a = r / nao;
+    for (int64_t j = 0; j < no; ++j) sum += fabsf(bra[nu + nao * j + nao * no * a]);
+  }
+  for (int o = 16; o > 0; o >>= 1) sum = fmaxf(sum, __shfl_xor_sync(0xffffffffu, sum, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(sum));
+}
+
+// *mx = an upper bound of |T_P[nu, (i,a)]| = |sum_j bra[nu,j,a] O_P[j,i]| over P in [0, npc):
+// (max_{nu,a} sum_j |bra|) (max_{P,j,i} |O_P|), rounded up (float bits); one block
+__global__ void tbound_kernel(const unsigned* __restrict__ bra_s, const unsigned* __restrict__ omax, int64_t npc,
+                              unsigned* __restrict__ mx) {
+  __shared__ float red[32];
+  float m = 0.f;
+  for (int64_t p = threadIdx.x; p < npc; p += blockDim.x) m = fmaxf(m, __uint_as_float(omax[p]));
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
+    *mx = __float_as_uint(__uint_as_float(*bra_s) * m * 1.0001f);
+  }
+}
+
 unsigned grid_for(int64_t total) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(div_up(total, 256), 1 << 20)); }
 unsigned grid_warps(int64_t rows, int num_sms) {
   return (unsigned)std::max<int64_t>(1, std::min<int64_t>(div_up(rows * 32, 256), 16 * (int64_t)num_sms));
@@ -731,10 +769,8 @@ bool set_smem_attr() {
          cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               Batched<PR>::SMEM_BYTES) == cudaSuccess &&
          (PR::S == 6 ||
-          (cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64, EPI_MAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                Batched<PR>::SMEM_BYTES) == cudaSuccess &&
-           cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64, EPI_SPLIT16>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, Batched<PR>::SMEM_BYTES) == cudaSuccess));
+          cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64, EPI_SPLIT16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               Batched<PR>::SMEM_BYTES) == cudaSuccess);
 }
 
 // ---- launch-shape autotuner ---------------------------------------------------------------
@@ -1114,7 +1150,10 @@ static void lp_prepare_spin(cphf_ctx* c, OzState& z, int s) {
                                                          Split2::EOFF, o.eZt.as<int>(), o.sZt.as<double>());
   slice_zt_kernel<Split2, float><<<grid_for(nao * no * naux), 256, 0, c->stream>>>(
       sp.Z32.as<float>(), nao, no, naux, ldj, o.eZt.as<int>(), o.Zt.as<__half>());
-  count_launch(5);
+  o.Omax.ensure((size_t)naux * 4, c->counter());
+  omax_kernel<<<(unsigned)std::min<int64_t>(naux, 65535), 256, 0, c->stream>>>(sp.O32.as<float>(), no * no, naux,
+                                                                              o.Omax.as<unsigned>());
+  count_launch(6);
   CPHF_CUDA(cudaGetLastError());
   o.ready = true;
 }
@@ -1135,31 +1174,12 @@ void lp_begin(cphf_ctx* c, OzState& z, int s, const float* bra, int64_t nb) {
     z.ebrat.ensure((size_t)nao * nb * 4, c->counter());
     slice_rows_kernel<Split2, float><<<grid_warps(nao * nb, c->num_sms), 256, 0, c->stream>>>(
         bra, nao * nb, no, nao, 1, nao * no, nao, z.brat.as<__half>(), ldj, nao * nb * ldj, z.ebrat.as<int>());
-    count_launch(2);
+    z.braS.ensure(sizeof(unsigned), c->counter());
+    CPHF_CUDA(cudaMemsetAsync(z.braS.p, 0, sizeof(unsigned), c->stream));
+    bra_rowsum_max_kernel<<<grid_for(nao * nb), 256, 0, c->stream>>>(bra, nao, no, nb, z.braS.as<unsigned>());
+    count_launch(3);
   }
   CPHF_CUDA(cudaGetLastError());
-}
-
-void lp_tgen(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, float* T32, int64_t ldt,
-             int* err) {
-  const int64_t nao = c->nao, naux = c->naux, no = c->spin[s].nocc, N = no * nb;
-  const int64_t ldj = z.spin[s].ldj;
-  constexpr int S2 = Split2::S;
-  const CUtensorMap mBt = make_map(z.brat.p, no, nao * nb, S2, ldj, BM, false);
-  const CUtensorMap mO = make_map(z.spin[s].O.p, no, no, S2 * naux, ldj, 64, false);
-  OzArgs a = base_args(z, (int)(nao * nb), (int)no);
-  a.err = err;
-  a.out = T32;
-  a.nkb = (int)div_up(no, BK);
-  a.a_depth = 1;
-  a.b_depth = (int)naux;
-  a.b_off = (int)P0;
-  a.e_row = z.ebrat.as<int>();
-  a.e_col = z.spin[s].eO.as<int>();
-  a.m_div = nao; a.s_m1 = 1; a.s_m2 = ldt * no; a.s_n = ldt; a.s_p = N * ldt;
-  ProfScope ps(c, PROF_TC_SPLIT, 2.0 * nao * nb * no * no * npc, 0.0);
-  a.np = (int)npc;
-  launch_batched<Split2>(c, mBt, mO, a);
 }
 
 void lp_tgen_planes(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, int64_t ldt, __half* hi,
@@ -1179,13 +1199,14 @@ void lp_tgen_planes(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int
   a.e_col = z.spin[s].eO.as<int>();
   a.m_div = nao; a.s_m1 = 1; a.s_m2 = ldt * no; a.s_n = ldt; a.s_p = N * ldt;
   a.np = (int)npc;
-  a.mx = mx;
   a.tscale = scale;
   a.out = hi;
   a.out_lo = lo;
-  ProfScope ps(c, PROF_TC_SPLIT, 2.0 * 2.0 * nao * nb * no * no * npc, 2.0 * 2.0 * npc * N * nao);
-  CPHF_CUDA(cudaMemsetAsync(mx, 0, sizeof(unsigned), c->stream));
-  launch_batched<Split2, EPI_MAX>(c, mBt, mO, a);
+  ProfScope ps(c, PROF_TC_SPLIT, 2.0 * nao * nb * no * no * npc, 2.0 * 2.0 * npc * N * nao);
+  // FP16 scale from an upper bound of |T| (hi and lo keep their 22 bits for values within
+  // 2^17 of the bound, so a loose bound costs nothing and saves a max pass over T)
+  tbound_kernel<<<1, 256, 0, c->stream>>>(z.braS.as<unsigned>(), z.spin[s].Omax.as<unsigned>() + P0, npc, mx);
+  count_launch();
   launch_t_scale(mx, sA, alpha, scale, c->stream);
   launch_batched<Split2, EPI_SPLIT16>(c, mBt, mO, a);
 }
@@ -1216,7 +1237,7 @@ void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t
     a.e_row = z.ebraw.as<int>();
     a.e_col = os.eZ.as<int>();
     a.m_div = no; a.s_m1 = 1; a.s_m2 = ldj * no; a.s_n = ldj; a.s_p = N * ldj;
-    ProfScope ps(c, PROF_TC_SPLIT, 2.0 * N * no * nao * npc, 0.0);
+    ProfScope ps(c, PROF_TC_WGEN, 2.0 * N * no * nao * npc, 0.0);
     a.np = (int)npc;
     launch_batched<Split2>(c, mBw, mZ, a);
   }
@@ -1247,7 +1268,7 @@ void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t
     a.rowscale = os.sZt.as<double>();
     a.colscale = z.colscale.as<double>();
     a.ld_out = nao;
-    ProfScope ps(c, PROF_TC_SPLIT, 2.0 * nao * N * no * npc, 2.0 * S2 * no * npc * (nao + N));
+    ProfScope ps(c, PROF_TC_TERM2, 2.0 * nao * N * no * npc, 2.0 * S2 * no * npc * (nao + N));
     launch_split<Split2, 128>(c, z, mZt, mW, a);
   }
 }

@@ -25,11 +25,8 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
 // inner solves' operator, from the FP32 copies of O and Z:
 // per call, the bra planes of spin s (bra FP32 [nao, nocc_s, nb])
 void lp_begin(cphf_ctx* c, OzState& z, int s, const float* bra, int64_t nb);
-// T[Pl][(i,a)][nu] (FP32, row stride ldt) = sum_j bra[nu,j,a] O_P[j,i] for P in [P0, P0 + npc)
-void lp_tgen(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, float* T32, int64_t ldt,
-             int* err);
-// the same T as FP16 hi / lo planes of s T (two passes: max |T| into *mx, launch_t_scale,
-// planes), hi and lo npc * nocc * nb * ldt apart in memory
+// T[Pl][(i,a)][nu] = sum_j bra[nu,j,a] O_P[j,i] for P in [P0, P0 + npc) as FP16 hi / lo planes
+// (row stride ldt) of s T; s from an upper bound of |T| written to *mx (launch_t_scale)
 void lp_tgen_planes(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, int64_t ldt, __half* hi,
                     __half* lo, unsigned* mx, float* scale, float sA, float alpha, int* err);
 // out (FP32 [nao, nocc_s, nb]) += alpha sum_{P in chunk} Z_P (Z_P^T bra)^T

@@ -34,23 +34,57 @@ struct XcCfg<float> {
 
 // Register-tiled product over one K range; loadA(m, k) / loadB(k, n) return 0 outside.
 // Operands are stored as T and converted to the compute type TC when staged (TC = dfloat:
-// FP64-accurate products on the FP32 pipes for the mixed solve's residual).
+// FP64-accurate products on the FP32 pipes for the mixed solve's residual).  The next K tile
+// is fetched into registers while the current one is multiplied out of shared memory (FP32
+// compute; for FP64 / double-float the extra registers cost more occupancy than they save).
 template <typename TC, typename Cfg, typename LA_, typename LB_>
 __device__ __forceinline__ void tile_accumulate(TC (&acc)[Cfg::TM][Cfg::TN], int64_t K, LA_ loadA, LB_ loadB,
                                                 TC (*As)[Cfg::BM], TC (*Bs)[Cfg::BN]) {
   constexpr int BM = Cfg::BM, BN = Cfg::BN, BK = Cfg::BK, TM = Cfg::TM, TN = Cfg::TN;
   constexpr int NTX = BN / TN, NTY = BM / TM, NT = NTX * NTY;
+  constexpr int RA = BM * BK / NT, RB = BK * BN / NT;
+  static_assert(BM * BK % NT == 0 && BK * BN % NT == 0, "tile / thread count");
   const int tid = threadIdx.x, tx = tid % NTX, ty = tid / NTX;
-  for (int64_t k0 = 0; k0 < K; k0 += BK) {
-    for (int e = tid; e < BM * BK; e += NT) {
-      const int mm = e % BM, kk = e / BM;
-      As[kk][mm] = (k0 + kk < K) ? TC(loadA(mm, k0 + kk)) : TC(0);
+  if (K <= 0) return;
+  TC ra[RA], rb[RB];
+  auto fetch = [&](int64_t k0) {
+#pragma unroll
+    for (int r = 0; r < RA; ++r) {
+      const int e = tid + r * NT, mm = e % BM, kk = e / BM;
+      ra[r] = (k0 + kk < K) ? TC(loadA(mm, k0 + kk)) : TC(0);
     }
-    for (int e = tid; e < BK * BN; e += NT) {
-      const int kk = e % BK, nn = e / BK;
-      Bs[kk][nn] = (k0 + kk < K) ? TC(loadB(k0 + kk, nn)) : TC(0);
+#pragma unroll
+    for (int r = 0; r < RB; ++r) {
+      const int e = tid + r * NT, kk = e % BK, nn = e / BK;
+      rb[r] = (k0 + kk < K) ? TC(loadB(k0 + kk, nn)) : TC(0);
+    }
+  };
+  constexpr bool PREFETCH = sizeof(TC) == 4;
+  if (PREFETCH) fetch(0);
+  for (int64_t k0 = 0; k0 < K; k0 += BK) {
+    if (PREFETCH) {
+#pragma unroll
+      for (int r = 0; r < RA; ++r) {
+        const int e = tid + r * NT;
+        As[e / BM][e % BM] = ra[r];
+      }
+#pragma unroll
+      for (int r = 0; r < RB; ++r) {
+        const int e = tid + r * NT;
+        Bs[e % BK][e / BK] = rb[r];
+      }
+    } else {
+      for (int e = tid; e < BM * BK; e += NT) {
+        const int mm = e % BM, kk = e / BM;
+        As[kk][mm] = (k0 + kk < K) ? TC(loadA(mm, k0 + kk)) : TC(0);
+      }
+      for (int e = tid; e < BK * BN; e += NT) {
+        const int kk = e % BK, nn = e / BK;
+        Bs[kk][nn] = (k0 + kk < K) ? TC(loadB(k0 + kk, nn)) : TC(0);
+      }
     }
     __syncthreads();
+    if (PREFETCH && k0 + BK < K) fetch(k0 + BK);
 #pragma unroll
     for (int kk = 0; kk < BK; ++kk) {
       TC a[TM], b[TN];
@@ -68,7 +102,7 @@ __device__ __forceinline__ void tile_accumulate(TC (&acc)[Cfg::TM][Cfg::TN], int
 }
 
 template <typename T, typename TC>
-__global__ void __launch_bounds__(256) xc_gemm1_kernel(const XcGroupDev* __restrict__ groups, int ngroups,
+__global__ void __launch_bounds__(256, sizeof(TC) == 4 ? 2 : 3) xc_gemm1_kernel(const XcGroupDev* __restrict__ groups, int ngroups,
                                                        const T* __restrict__ phi, const T* __restrict__ bra,
                                                        int64_t nao, int64_t N, int64_t pchunk, T* __restrict__ ket,
                                                        int64_t total_tiles, int64_t tiles_n) {
@@ -114,7 +148,7 @@ __global__ void __launch_bounds__(256) xc_gemm1_kernel(const XcGroupDev* __restr
 }
 
 template <typename T, typename TC>
-__global__ void __launch_bounds__(256) xc_gemm2_kernel(const XcGroupDev* __restrict__ groups, int ngroups,
+__global__ void __launch_bounds__(256, sizeof(TC) == 4 ? 2 : 3) xc_gemm2_kernel(const XcGroupDev* __restrict__ groups, int ngroups,
                                                        const T* __restrict__ phi, const T* __restrict__ q,
                                                        int64_t nao, int64_t N, int64_t pchunk, T* __restrict__ out,
                                                        double alpha, double beta, int64_t tiles_m, int64_t tiles_n) {
