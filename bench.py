@@ -387,13 +387,20 @@ def run_gpu(args, world, rank, local):
                                 f"FLOPs" + (f"; {note}" if note else ""))
     # DRAM bytes per launch: the ratio of ncu-measured DRAM bytes to the algorithmic bytes of
     # the same kernel on a small case (profiles/), times this run's algorithmic bytes per launch
-    traffic_ratio = {"kterm_tcgen05_f16x3": 1.262 / 1.18}   # tc_term1_kernel, rhf_nao300
+    traffic_ratio = {"kterm_tcgen05_f16x3": 1.262 / 1.18,        # tc_term1_kernel, rhf_nao300
+                     "kterm_tcgen05_bf16x6_exact": 5.954 / 5.22}  # tc_slice_kernel<Exact6>, rhf_nao300
     traffic = None
     if dom_name in traffic_ratio and dom.get("bytes", 0) > 0:
         traffic = traffic_ratio[dom_name] * dom["bytes"] / dom["launches"]
     if dom_name.startswith("xc_grouped"):
         roof.update(bound="fp64 pipe" if dom_name.endswith("fp64") else "fp32 pipe", peak=None,
                     peak_source="SIMT GEMM (no tensor-core form); see the per-class TFLOP/s")
+    # products the tensor pipe executes per algorithmic FLOP (slices x slices kept)
+    products = {"kterm_tcgen05_f16x3": 3, "tgen_tcgen05_f16x3": 3, "wgen_tcgen05_f16x3": 3,
+                "term2_tcgen05_f16x3": 3, "kterm_tcgen05_bf16x6_exact": 21}.get(dom_name)
+    if products and roof.get("peak"):
+        roof.update(tensor_executed_tflops=roof["achieved"] * products,
+                    tensor_executed_frac=roof["achieved"] * products / roof["peak"])
     roof.update(kernel=dom_name, frac=roof["achieved"] / roof["peak"] if roof.get("peak") else None, traffic=traffic,
                 traffic_unit="bytes per launch" if traffic else None,
                 launches=dom["launches"], avg_launch_ms=dom["ms"] / dom["launches"],

@@ -1,5 +1,4 @@
 // Element-wise, reduction and small dense-algebra kernels, see kernels.cuh.
-#include <cuda_bf16.h>
 
 #include <algorithm>
 
@@ -342,17 +341,6 @@ __global__ void lu_backsub_kernel(const double* __restrict__ h, int64_t ldh, dou
   if (threadIdx.x == 0) g[k + ldg * c] = x;
 }
 
-__global__ void split_bf16_kernel(const double* __restrict__ src, int64_t n,
-                                  __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const double v = src[t];
-    const __nv_bfloat16 h = __double2bfloat16(v);
-    hi[t] = h;
-    lo[t] = __double2bfloat16(v - (double)__bfloat162float(h));
-  }
-}
-
 __global__ void axpby_kernel(double alpha, const double* __restrict__ x, double beta,
                              double* __restrict__ y, int64_t n) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
@@ -487,11 +475,6 @@ void launch_lu_solve(double* h, int64_t ldh, double* g, int64_t ldg, int64_t m, 
     lu_backsub_kernel<<<(unsigned)nrhs, kThreads, 0, s>>>(h, ldh, g, ldg, k);
     count_launch();
   }
-}
-
-void launch_split_bf16(const double* src, int64_t n, void* hi, void* lo, cudaStream_t s) {
-  split_bf16_kernel<<<grid_for(n), kThreads, 0, s>>>(src, n, (__nv_bfloat16*)hi, (__nv_bfloat16*)lo);
-  count_launch();
 }
 
 void launch_axpby(double alpha, const double* x, double beta, double* y, int64_t n, cudaStream_t s) {

@@ -66,8 +66,6 @@ void launch_add_diag(double* h, int64_t ldh, const double* ip, int64_t m, cudaSt
 void launch_lu_solve(double* h, int64_t ldh, double* g, int64_t ldg, int64_t m, int64_t nrhs,
                      int* info, cudaStream_t s);
 
-// Split FP64 -> (hi, lo) bf16 pairs with optional transposition handled by the caller.
-void launch_split_bf16(const double* src, int64_t n, void* hi, void* lo, cudaStream_t s);
 
 // y = alpha x + beta y over n elements
 void launch_axpby(double alpha, const double* x, double beta, double* y, int64_t n,
