@@ -35,6 +35,16 @@ struct OzState {
   bool ready = false;
 };
 
+// Dense split-FP16 forms of phi for the tensor-core XC response (xc_tc.cu).
+struct XcTcState {
+  DevBuf batches, pt_batch;   // batch records and the batch of every grid point
+  DevBuf phiA, phiA_scale;    // [2][ngrids][ldk] planes of phi rows p, scale per point
+  DevBuf phiT, phiT_scale;    // per chunk: [2][nao][ldq] planes of phi^T, scale per AO
+  DevBuf bpl[2], eb[2], bscale[2];  // planes of bra rows (i, a) per spin, their exponents and scales
+  DevBuf qpl, eq, qscale;
+  bool ready = false;
+};
+
 // One captured application of the split-precision operator for block width nb, reading and
 // writing the staging buffers of LowpState (g_x, g_y).
 struct OpGraph {
@@ -49,6 +59,7 @@ struct LowpState {
   int64_t ldk = 0;             // padded row length of the FP16 copies
   OzState oz;                  // FP64-accurate tensor-core K term of the residual
   OzState lp;                  // split-FP16 planes of O, Z and bra for the K term's other contractions
+  XcTcState xctc;              // dense split-FP16 phi for the tensor-core XC response
   DevBuf phi32;
   DevBuf s_c1, s_resp, s_T, s_W, s_d, s_ket, s_rho, s_y, s_x, s_Thi, s_Tlo, s_acc;
   DevBuf err;                  // device error flag of the tensor-core kernels (bounded waits)

@@ -18,6 +18,7 @@
 #include "tc_gemm.cuh"
 #include "tc_ozaki.cuh"
 #include "xc_grouped.cuh"
+#include "xc_tc.cuh"
 
 namespace cphf {
 
@@ -175,6 +176,10 @@ static void rijk_response_lowp(cphf_ctx* c, float* const* bra, int64_t nb, float
 
 static void xc_response_lowp(cphf_ctx* c, float* const* bra, int64_t nb, float* const* out, bool accumulate) {
   LowpState& L = *c->lowp;
+  if (L.use_tc) {
+    xc_response_tc(c, bra, nb, out, accumulate);
+    return;
+  }
   const float* aobra[2] = {c->spin[0].aobra32.as<float>(), c->nspin > 1 ? c->spin[1].aobra32.as<float>() : nullptr};
   xc_response_grouped<float>(c, bra, nb, out, accumulate, L.phi32.as<float>(), aobra, L.s_ket, L.s_rho);
 }

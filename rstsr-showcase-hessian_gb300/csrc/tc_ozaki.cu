@@ -97,6 +97,7 @@ struct OzArgs {
   int a_depth, b_depth;     // plane stride of A / B in depth units (slice t at depth t * stride)
   int a_off, b_off;         // depth offset of the chunk's aux function 0
   int a_per_p;              // A depth advances with the aux function
+  int a_row0;               // split mode: first A row of the contraction (A rows need no alignment)
   int np, p_per_cta;        // batched: aux functions of the launch, per CTA
   int kb_per_cta;           // split: K blocks per CTA (<= KMAX / BK, the exactness bound)
   // batched split-FP16 T generation writing the FP16 hi / lo planes of T * (*tscale) for
@@ -186,7 +187,7 @@ __global__ void __launch_bounds__(128, 1)
         const uint32_t st = smem_u32(smem + s * C::STAGE_BYTES);
 #pragma unroll
         for (int t = 0; t < PR::S; ++t) {
-          tma_load_3d(st + t * C::A_TILE, &mA, full, k0, m0, t * args.a_depth + da);
+          tma_load_3d(st + t * C::A_TILE, &mA, full, k0, m0 + args.a_row0, t * args.a_depth + da);
           tma_load_3d(st + PR::S * C::A_TILE + t * C::B_TILE, &mB, full, k0, n0, t * args.b_depth + db);
         }
       }
@@ -840,7 +841,7 @@ template <class PR, int BN>
 void launch_split(cphf_ctx* c, OzState& z, const CUtensorMap& mA, const CUtensorMap& mB, OzArgs a) {
   const TuneKey key{PR::S * 1000 + BN, a.M, a.N, a.nkb, a.total_kb};
   auto& tab = tune_table();
-  int best = KB_PER_CTA;
+  int best = PR::NACC == 1 ? (int)std::max<int64_t>(1, div_up(a.total_kb, 4)) : KB_PER_CTA;
   if (!tab.find(key, best) && !capturing(c->stream)) {
     // candidates run into a scratch output (the real one accumulates)
     const size_t esize = PR::NACC == 4 ? 8 : 4;
@@ -849,7 +850,16 @@ void launch_split(cphf_ctx* c, OzState& z, const CUtensorMap& mA, const CUtensor
     OzArgs t = a;
     t.out = z.tune_out.p;
     float best_ms = 0.f;
-    for (int kb : {KB_PER_CTA, KB_PER_CTA / 2, KB_PER_CTA / 3}) {
+    // exact slices: K ranges within the exactness bound; split FP16 (no bound): 1, 2 or 4
+    // waves of CTAs over the tiles, each K range as long as that leaves it
+    int cand[3] = {KB_PER_CTA, KB_PER_CTA / 2, KB_PER_CTA / 3};
+    if (PR::NACC == 1) {
+      const int64_t tiles = (int64_t)a.m_tiles * div_up(a.N, BN);
+      const int64_t r0 = std::max<int64_t>(1, div_up(2 * (int64_t)c->num_sms, tiles));
+      for (int q = 0; q < 3; ++q)
+        cand[q] = (int)std::max<int64_t>(1, div_up(a.total_kb, std::min<int64_t>(r0 << q, a.total_kb)));
+    }
+    for (int kb : cand) {
       t.kb_per_cta = kb;
       if (div_up(t.total_kb, kb) > 65535) continue;
       const float ms = time_launch(c->stream, [&] { launch_split_raw<PR, BN>(c, mA, mB, t); });
@@ -1271,6 +1281,53 @@ void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t
     ProfScope ps(c, PROF_TC_TERM2, 2.0 * nao * N * no * npc, 2.0 * S2 * no * npc * (nao + N));
     launch_split<Split2, 128>(c, z, mZt, mW, a);
   }
+}
+
+// Split-FP16 contraction out[m, n] += rowscale[m] colscale[n] sum_k A[a_row0 + m, k] B[n, k]
+// over FP16 hi / lo planes (plane stride rows x ld elements), K-major, FP32 atomics into out
+// [m + ld_out n]; the K range is split over CTAs as the autotuner finds best.
+void lp_gemm(cphf_ctx* c, OzState& z, const __half* A, int64_t a_rows, int64_t a_ld, int64_t a_row0,
+             const __half* B, int64_t b_rows, int64_t b_ld, int64_t M, int64_t N, int64_t K,
+             const double* rowscale, const double* colscale, float* out, int64_t ld_out, int* err) {
+  if (M <= 0 || N <= 0 || K <= 0) return;
+  const CUtensorMap mA = make_map(A, K, a_rows, Split2::S, a_ld, BM, false);
+  const CUtensorMap mB = make_map(B, K, b_rows, Split2::S, b_ld, BM, false);
+  OzArgs a = base_args(z, (int)M, (int)N);
+  a.err = err;
+  a.out = out;
+  a.nkb = (int)div_up(K, BK);
+  a.total_kb = a.nkb;
+  a.a_depth = 1;
+  a.b_depth = 1;
+  a.a_row0 = (int)a_row0;
+  a.rowscale = rowscale;
+  a.colscale = colscale;
+  a.ld_out = ld_out;
+  launch_split<Split2, 128>(c, z, mA, mB, a);
+}
+
+// Split-FP16 planes of bra rows (j, a) over nu (the W-generation / XC A-or-B operand) only.
+void lp_slice_braw(cphf_ctx* c, OzState& z, int s, const float* bra, int64_t nb) {
+  const int64_t nao = c->nao, no = c->spin[s].nocc, N = no * nb;
+  z.ldk = (nao + 7) / 8 * 8;
+  const int64_t ldk = z.ldk;
+  z.braw.ensure((size_t)Split2::S * N * ldk * 2, c->counter());
+  z.ebraw.ensure((size_t)N * 4, c->counter());
+  ProfScope ps_slice(c, PROF_SLICE, 0.0, 8.0 * N * nao + 4.0 * N * ldk);
+  slice_rows_kernel<Split2, float><<<grid_warps(N, c->num_sms), 256, 0, c->stream>>>(
+      bra, N, nao, 0, nao, 0, 1, z.braw.as<__half>(), ldk, N * ldk, z.ebraw.as<int>());
+  count_launch();
+  CPHF_CUDA(cudaGetLastError());
+}
+
+// Split-FP16 planes [t][r][ld] of FP32 rows r (K elements each, row stride rs), exponents to e_out.
+void lp_slice_rows(cphf_ctx* c, const float* src, int64_t rows, int64_t K, int64_t rs, __half* dst, int64_t ld,
+                   int* e_out) {
+  ProfScope ps_slice(c, PROF_SLICE, 0.0, 4.0 * rows * K + 4.0 * rows * ld);
+  slice_rows_kernel<Split2, float><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(
+      src, rows, K, 0, rs, 0, 1, dst, ld, rows * ld, e_out);
+  count_launch();
+  CPHF_CUDA(cudaGetLastError());
 }
 
 }  // namespace cphf

@@ -33,4 +33,17 @@ void lp_tgen_planes(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int
 void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, double alpha, float* out,
                 int* err);
 
+// Split-FP16 contraction out[m, n] += rowscale[m] colscale[n] sum_k A[a_row0 + m, k] B[n, k]:
+// A, B FP16 hi / lo planes (K-major rows of ld elements; lo plane rows x ld elements after hi),
+// out FP32 [m + ld_out n] accumulated with atomics.
+void lp_gemm(cphf_ctx* c, OzState& z, const __half* A, int64_t a_rows, int64_t a_ld, int64_t a_row0,
+             const __half* B, int64_t b_rows, int64_t b_ld, int64_t M, int64_t N, int64_t K,
+             const double* rowscale, const double* colscale, float* out, int64_t ld_out, int* err);
+
+// split-FP16 planes of bra's rows (j, a) over nu into z.braw (exponents z.ebraw) only
+void lp_slice_braw(cphf_ctx* c, OzState& z, int s, const float* bra, int64_t nb);
+// split-FP16 planes [t][r][ld] of FP32 rows r (K elements each, row stride rs); row exponents to e_out
+void lp_slice_rows(cphf_ctx* c, const float* src, int64_t rows, int64_t K, int64_t rs, __half* dst, int64_t ld,
+                   int* e_out);
+
 }  // namespace cphf

@@ -247,7 +247,7 @@ int64_t xc_tiles_n(int64_t N, bool f64) { return div_up(N, f64 ? XcCfg<double>::
 // Chunks of consecutive batches whose intermediates (ket of every spin) fit the budget; one
 // cached plan per (precision, chunk cap, nb, nocc) so that the block widths of a Krylov solve
 // each keep theirs (captured operator graphs read the plan's device records).
-static XcPlan& xc_plan(cphf_ctx* c, size_t esize, int64_t nb) {
+XcPlan& xc_plan(cphf_ctx* c, size_t esize, int64_t nb) {
   const bool f64 = esize == 8;
   const int ns = c->nspin;
   const int64_t key[4] = {(int64_t)esize * 1000003 + c->cfg.xc_chunk_points, nb, c->spin[0].nocc,

@@ -27,6 +27,8 @@ void xc_grouped_gemm1(cphf_ctx* c, const XcGroupDev* groups_dev, int ngroups, in
 template <typename T>
 void xc_grouped_gemm2(cphf_ctx* c, const XcGroupDev* groups_dev, int ngroups, const T* phi, const T* q, int64_t N,
                       int64_t pchunk, T* out, double alpha, double beta);
+// chunk plan of the grid batches for element size esize and nb columns (cached per width)
+XcPlan& xc_plan(cphf_ctx* c, size_t esize, int64_t nb);
 int64_t xc_tiles_m(int64_t npts, bool f64);
 int64_t xc_tiles_n(int64_t N, bool f64);
 

@@ -213,7 +213,7 @@ TC_RAGGED = dict(nao=150, naux=70, nocc=(13,), natm=9, decay=12.0)
 
 
 @pytest.mark.parametrize("tc", [1, 0])
-@pytest.mark.parametrize("dims", [MEDIUM, TC_RAGGED, MEDIUM_U, GRID_R])
+@pytest.mark.parametrize("dims", [MEDIUM, TC_RAGGED, MEDIUM_U, GRID_R, GRID_U])
 def test_lowp_operator_accuracy(dims, tc):
     """The split-precision operator of the mixed solve agrees with FP64 to LOWP_TOL."""
     s = synth.make_system(dims, seed=14)
