@@ -60,6 +60,7 @@ struct LowpState {
   OzState oz;                  // FP64-accurate tensor-core K term of the residual
   OzState lp;                  // split-FP16 planes of O, Z and bra for the K term's other contractions
   XcTcState xctc;              // dense split-FP16 phi for the tensor-core XC response
+  XcTcState xctc64;            // dense exact-slice phi for the FP64-accurate XC residual
   DevBuf phi32;
   DevBuf s_c1, s_resp, s_T, s_W, s_d, s_ket, s_rho, s_y, s_x, s_Thi, s_Tlo, s_acc;
   DevBuf err;                  // device error flag of the tensor-core kernels (bounded waits)
@@ -160,7 +161,9 @@ enum ProfClass {
   PROF_XC32 = 9,
   PROF_TC_WGEN = 10,
   PROF_TC_TERM2 = 11,
-  PROF_NCLASS = 12
+  PROF_XC_TC32 = 12,
+  PROF_XC_TC64 = 13,
+  PROF_NCLASS = 14
 };
 extern const char* const kProfNames[PROF_NCLASS];
 
@@ -206,6 +209,7 @@ struct cphf_ctx {
   cphf::Profiler prof;
   bool f64_emulate = false;  // route the FP64 GEMMs through the double-float kernel
   bool oz_kterm = false;     // FP64 K term 1 on the tensor cores (exact BF16 slices)
+  bool oz_xc = false;        // FP64 XC response on the tensor cores (exact BF16 slices)
 
   int64_t* counter() { return &device_bytes; }
 };

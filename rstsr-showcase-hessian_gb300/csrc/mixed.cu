@@ -398,15 +398,18 @@ bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, d
       c->f64_emulate = c->cfg.residual_dfloat != 0;
       c->oz_kterm = c->cfg.residual_dfloat == 2 && c->has_rijk && c->lowp->use_tc && oz_available(c) &&
                     oz_supported(c);
+      c->oz_xc = c->cfg.residual_dfloat == 2 && c->has_xc && c->lowp->use_tc && oz_available(c);
       try {
         res = fp64_residual(c, b, x, nset, r, st);
       } catch (...) {
         c->f64_emulate = false;
         c->oz_kterm = false;
+        c->oz_xc = false;
         throw;
       }
       c->f64_emulate = false;
       c->oz_kterm = false;
+      c->oz_xc = false;
       done = res < c->cfg.residual_tol;
     } else {
       lowp_apply(c, dlt, nset, adl);

@@ -27,7 +27,8 @@ const char* const kProfNames[PROF_NCLASS] = {"gemm_fp64_simt", "gemm_fp32_simt",
                                              "gemm_fp64_dfloat", "kterm_tcgen05_bf16x6_exact",
                                              "tgen_tcgen05_f16x3", "slice_scale_split",
                                              "krylov_mgs_lu", "xc_grouped_fp64", "xc_grouped_fp32",
-                                             "wgen_tcgen05_f16x3", "term2_tcgen05_f16x3"};
+                                             "wgen_tcgen05_f16x3", "term2_tcgen05_f16x3",
+                                             "xc_tcgen05_f16x3", "xc_tcgen05_bf16x6_exact"};
 
 static double gemm_flops(const GemmDesc& d) { return 2.0 * d.M * d.N * d.K * d.batch1 * d.batch2; }
 

@@ -1,0 +1,124 @@
+// Operand representations of the tensor-core contractions and their slicing primitives
+// (integer arithmetic on the FP64 / FP32 bit patterns), shared by the K-term kernels
+// (tc_ozaki.cu) and the XC response (xc_tc.cu).
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <cstdint>
+#include <type_traits>
+
+namespace cphf {
+
+// Operand representations: exact BF16 slices (FP64-accurate residual) and split FP16 hi/lo
+// (the inner solves' operator).  EOFF: exponent offset of the stored planes (x 2^(EOFF - e)).
+struct Exact6 {
+  static constexpr int S = 6, NACC = 4, EOFF = 0, STAGES = 2;
+  static constexpr bool BF16 = true;
+  using Elem = __nv_bfloat16;
+};
+struct Split2 {
+  static constexpr int S = 2, NACC = 1, EOFF = 14, STAGES = 6;
+  static constexpr bool BF16 = false;
+  using Elem = __half;
+};
+
+// ---- slicing (integer arithmetic on the bit patterns; the FP64 pipe is not used) ----------
+// |x| as an ordered integer key (non-negative floats order like their bit patterns)
+__device__ __forceinline__ unsigned long long abs_key(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+__device__ __forceinline__ unsigned long long abs_key(float2 x) {
+  return (unsigned long long)(__float_as_uint(x.x) & 0x7FFFFFFFu);
+}
+__device__ __forceinline__ unsigned long long abs_key(float x) {
+  return (unsigned long long)(__float_as_uint(x) & 0x7FFFFFFFu);
+}
+template <class T>
+__host__ __device__ constexpr bool float_key() { return !std::is_same<T, double>::value; }
+
+// round(x 2^k) for |x| 2^k <= 2^36, from the FP64 bit pattern
+__device__ __forceinline__ long long fix_round(double x, int k, bool& bad) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  const int E = (int)((bits >> 52) & 0x7FF);
+  if (E == 0x7FF) { bad = true; return 0; }
+  const long long M = E ? (long long)((bits & 0xFFFFFFFFFFFFFull) | (1ull << 52)) : (long long)(bits & 0xFFFFFFFFFFFFFull);
+  const int sh = 1075 - k - (E ? E : 1);  // x = M 2^(E - 1075)
+  long long F = 0;
+  if (sh <= 0) F = M << min(-sh, 10);
+  else if (sh < 63) F = (M + (1ll << (sh - 1))) >> sh;
+  return (bits >> 63) ? -F : F;
+}
+// same from the FP32 bit pattern
+__device__ __forceinline__ long long fix_round(float x, int k, bool& bad) {
+  const unsigned bits = __float_as_uint(x);
+  const int E = (int)((bits >> 23) & 0xFF);
+  if (E == 0xFF) { bad = true; return 0; }
+  const long long M = E ? (long long)((bits & 0x7FFFFFu) | 0x800000u) : (long long)(bits & 0x7FFFFFu);
+  const int sh = 150 - k - (E ? E : 1);   // x = M 2^(E - 150)
+  long long F = 0;
+  if (sh <= 0) F = M << min(-sh, 40);
+  else if (sh < 63) F = (M + (1ll << (sh - 1))) >> sh;
+  return (bits >> 31) ? -F : F;
+}
+
+// F = round(v 2^36), |F| <= 2^36, into the six digits q_t = round(R_t / 2^(30 - 6t)) of the
+// running remainder, written as BF16 slices q_t 2^(-6(t+1)) (plane stride `plane`).
+__device__ __forceinline__ void digits6(long long F, bool bad, __nv_bfloat16* dst, int64_t plane) {
+  long long R = F;
+#pragma unroll
+  for (int t = 0; t < Exact6::S; ++t) {
+    const int s = 30 - 6 * t;
+    const long long q = s > 0 ? ((R + (1ll << (s - 1))) >> s) : R;
+    R -= q << s;
+    float v = (float)(int)q * __int_as_float((127 - 6 * (t + 1)) << 23);  // q 2^(-6(t+1)), exact
+    if (bad) v = __int_as_float(0x7FC00000);                                // NaN / Inf propagate as NaN
+    dst[t * plane] = __float2bfloat16_rn(v);
+  }
+}
+__device__ __forceinline__ void slice6(double x, int e, __nv_bfloat16* dst, int64_t plane) {
+  bool bad = false;
+  const long long F = fix_round(x, 36 - e, bad);
+  digits6(F, bad, dst, plane);
+}
+__device__ __forceinline__ void slice6(float2 x, int e, __nv_bfloat16* dst, int64_t plane) {
+  bool bad = false;
+  const long long F = fix_round(x.x, 36 - e, bad) + fix_round(x.y, 36 - e, bad);
+  digits6(F, bad, dst, plane);
+}
+
+// store one element's planes: exact BF16 slices, or split FP16 hi/lo of x 2^(14 - e)
+template <class PR>
+struct Put;
+template <>
+struct Put<Exact6> {
+  template <class T>
+  __device__ static void put(T x, int e, __nv_bfloat16* dst, int64_t plane) { slice6(x, e, dst, plane); }
+};
+template <>
+struct Put<Split2> {
+  __device__ static void put(float x, int e, __half* dst, int64_t plane) {
+    const float v = ldexpf(x, Split2::EOFF - e);
+    const __half h = __float2half_rn(v);
+    dst[0] = h;
+    dst[plane] = __float2half_rn(v - __half2float(h));
+  }
+};
+
+// power of two strictly above max |x| (exponent e with max = f 2^e, f in [0.5, 1)); 0 for zero
+__device__ __forceinline__ int key_exp(unsigned long long key, bool is_float) {
+  if (is_float) {
+    const int E = (int)((key >> 23) & 0xFF);
+    if (key == 0 || E == 0xFF) return 0;
+    int e;
+    frexpf(__uint_as_float((unsigned)key), &e);
+    return e;
+  }
+  const int E = (int)((key >> 52) & 0x7FF);
+  if (key == 0 || E == 0x7FF) return 0;
+  int e;
+  frexp(__longlong_as_double((long long)key), &e);
+  return e;
+}
+
+}  // namespace cphf

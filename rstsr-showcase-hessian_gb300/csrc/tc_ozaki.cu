@@ -53,6 +53,7 @@
 #include "kernels.cuh"
 #include "tc_gemm.cuh"
 #include "tc_ozaki.cuh"
+#include "slices.cuh"
 #include "tc_ptx.cuh"
 
 namespace cphf {
@@ -63,18 +64,6 @@ constexpr int BM = 128, BK = 32;
 constexpr int KMAX = 3072;         // exactness bound of the K range of one CTA
 constexpr int KB_PER_CTA = KMAX / BK;
 
-// Operand representations: exact BF16 slices (FP64-accurate residual) and split FP16 hi/lo
-// (the inner solves' operator).  EOFF: exponent offset of the stored planes (x 2^(EOFF - e)).
-struct Exact6 {
-  static constexpr int S = 6, NACC = 4, EOFF = 0, STAGES = 2;
-  static constexpr bool BF16 = true;
-  using Elem = __nv_bfloat16;
-};
-struct Split2 {
-  static constexpr int S = 2, NACC = 1, EOFF = 14, STAGES = 6;
-  static constexpr bool BF16 = false;
-  using Elem = __half;
-};
 constexpr int S = Exact6::S;
 
 template <class PR, int BN>
@@ -480,104 +469,6 @@ __global__ void __launch_bounds__(320, PR::S == 6 ? 1 : 2)
   __syncthreads();
   fence_after_sync();
   if (warp == 1) tmem_dealloc(tmem, 2 * ACC);
-}
-
-// ---- slicing (integer arithmetic on the bit patterns; the FP64 pipe is not used) ----------
-// |x| as an ordered integer key (non-negative floats order like their bit patterns)
-__device__ __forceinline__ unsigned long long abs_key(double x) {
-  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
-}
-__device__ __forceinline__ unsigned long long abs_key(float2 x) {
-  return (unsigned long long)(__float_as_uint(x.x) & 0x7FFFFFFFu);
-}
-__device__ __forceinline__ unsigned long long abs_key(float x) {
-  return (unsigned long long)(__float_as_uint(x) & 0x7FFFFFFFu);
-}
-template <class T>
-__host__ __device__ constexpr bool float_key() { return !std::is_same<T, double>::value; }
-
-// round(x 2^k) for |x| 2^k <= 2^36, from the FP64 bit pattern
-__device__ __forceinline__ long long fix_round(double x, int k, bool& bad) {
-  const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
-  const int E = (int)((bits >> 52) & 0x7FF);
-  if (E == 0x7FF) { bad = true; return 0; }
-  const long long M = E ? (long long)((bits & 0xFFFFFFFFFFFFFull) | (1ull << 52)) : (long long)(bits & 0xFFFFFFFFFFFFFull);
-  const int sh = 1075 - k - (E ? E : 1);  // x = M 2^(E - 1075)
-  long long F = 0;
-  if (sh <= 0) F = M << min(-sh, 10);
-  else if (sh < 63) F = (M + (1ll << (sh - 1))) >> sh;
-  return (bits >> 63) ? -F : F;
-}
-// same from the FP32 bit pattern
-__device__ __forceinline__ long long fix_round(float x, int k, bool& bad) {
-  const unsigned bits = __float_as_uint(x);
-  const int E = (int)((bits >> 23) & 0xFF);
-  if (E == 0xFF) { bad = true; return 0; }
-  const long long M = E ? (long long)((bits & 0x7FFFFFu) | 0x800000u) : (long long)(bits & 0x7FFFFFu);
-  const int sh = 150 - k - (E ? E : 1);   // x = M 2^(E - 150)
-  long long F = 0;
-  if (sh <= 0) F = M << min(-sh, 40);
-  else if (sh < 63) F = (M + (1ll << (sh - 1))) >> sh;
-  return (bits >> 31) ? -F : F;
-}
-
-// F = round(v 2^36), |F| <= 2^36, into the six digits q_t = round(R_t / 2^(30 - 6t)) of the
-// running remainder, written as BF16 slices q_t 2^(-6(t+1)) (plane stride `plane`).
-__device__ __forceinline__ void digits6(long long F, bool bad, __nv_bfloat16* dst, int64_t plane) {
-  long long R = F;
-#pragma unroll
-  for (int t = 0; t < S; ++t) {
-    const int s = 30 - 6 * t;
-    const long long q = s > 0 ? ((R + (1ll << (s - 1))) >> s) : R;
-    R -= q << s;
-    float v = (float)(int)q * __int_as_float((127 - 6 * (t + 1)) << 23);  // q 2^(-6(t+1)), exact
-    if (bad) v = __int_as_float(0x7FC00000);                                // NaN / Inf propagate as NaN
-    dst[t * plane] = __float2bfloat16_rn(v);
-  }
-}
-__device__ __forceinline__ void slice6(double x, int e, __nv_bfloat16* dst, int64_t plane) {
-  bool bad = false;
-  const long long F = fix_round(x, 36 - e, bad);
-  digits6(F, bad, dst, plane);
-}
-__device__ __forceinline__ void slice6(float2 x, int e, __nv_bfloat16* dst, int64_t plane) {
-  bool bad = false;
-  const long long F = fix_round(x.x, 36 - e, bad) + fix_round(x.y, 36 - e, bad);
-  digits6(F, bad, dst, plane);
-}
-
-// store one element's planes: exact BF16 slices, or split FP16 hi/lo of x 2^(14 - e)
-template <class PR>
-struct Put;
-template <>
-struct Put<Exact6> {
-  template <class T>
-  __device__ static void put(T x, int e, __nv_bfloat16* dst, int64_t plane) { slice6(x, e, dst, plane); }
-};
-template <>
-struct Put<Split2> {
-  __device__ static void put(float x, int e, __half* dst, int64_t plane) {
-    const float v = ldexpf(x, Split2::EOFF - e);
-    const __half h = __float2half_rn(v);
-    dst[0] = h;
-    dst[plane] = __float2half_rn(v - __half2float(h));
-  }
-};
-
-// power of two strictly above max |x| (exponent e with max = f 2^e, f in [0.5, 1)); 0 for zero
-__device__ __forceinline__ int key_exp(unsigned long long key, bool is_float) {
-  if (is_float) {
-    const int E = (int)((key >> 23) & 0xFF);
-    if (key == 0 || E == 0xFF) return 0;
-    int e;
-    frexpf(__uint_as_float((unsigned)key), &e);
-    return e;
-  }
-  const int E = (int)((key >> 52) & 0x7FF);
-  if (key == 0 || E == 0x7FF) return 0;
-  int e;
-  frexp(__longlong_as_double((long long)key), &e);
-  return e;
 }
 
 // Generic row slicer: row r, element k at src[(r % rdiv) rs1 + (r / rdiv) rs2 + k ks]
@@ -1286,12 +1177,13 @@ void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t
 // Split-FP16 contraction out[m, n] += rowscale[m] colscale[n] sum_k A[a_row0 + m, k] B[n, k]
 // over FP16 hi / lo planes (plane stride rows x ld elements), K-major, FP32 atomics into out
 // [m + ld_out n]; the K range is split over CTAs as the autotuner finds best.
-void lp_gemm(cphf_ctx* c, OzState& z, const __half* A, int64_t a_rows, int64_t a_ld, int64_t a_row0,
-             const __half* B, int64_t b_rows, int64_t b_ld, int64_t M, int64_t N, int64_t K,
-             const double* rowscale, const double* colscale, float* out, int64_t ld_out, int* err) {
+template <class PR, class TOut>
+void plane_gemm(cphf_ctx* c, OzState& z, const typename PR::Elem* A, int64_t a_rows, int64_t a_ld, int64_t a_row0,
+                const typename PR::Elem* B, int64_t b_rows, int64_t b_ld, int64_t M, int64_t N, int64_t K,
+                const double* rowscale, const double* colscale, TOut* out, int64_t ld_out, int* err) {
   if (M <= 0 || N <= 0 || K <= 0) return;
-  const CUtensorMap mA = make_map(A, K, a_rows, Split2::S, a_ld, BM, false);
-  const CUtensorMap mB = make_map(B, K, b_rows, Split2::S, b_ld, BM, false);
+  const CUtensorMap mA = make_map(A, K, a_rows, PR::S, a_ld, BM, PR::BF16);
+  const CUtensorMap mB = make_map(B, K, b_rows, PR::S, b_ld, BM, PR::BF16);
   OzArgs a = base_args(z, (int)M, (int)N);
   a.err = err;
   a.out = out;
@@ -1303,7 +1195,19 @@ void lp_gemm(cphf_ctx* c, OzState& z, const __half* A, int64_t a_rows, int64_t a
   a.rowscale = rowscale;
   a.colscale = colscale;
   a.ld_out = ld_out;
-  launch_split<Split2, 128>(c, z, mA, mB, a);
+  launch_split<PR, 128>(c, z, mA, mB, a);
+}
+
+void lp_gemm(cphf_ctx* c, OzState& z, const __half* A, int64_t a_rows, int64_t a_ld, int64_t a_row0,
+             const __half* B, int64_t b_rows, int64_t b_ld, int64_t M, int64_t N, int64_t K,
+             const double* rowscale, const double* colscale, float* out, int64_t ld_out, int* err) {
+  plane_gemm<Split2>(c, z, A, a_rows, a_ld, a_row0, B, b_rows, b_ld, M, N, K, rowscale, colscale, out, ld_out, err);
+}
+
+void oz_gemm(cphf_ctx* c, OzState& z, const __nv_bfloat16* A, int64_t a_rows, int64_t a_ld, int64_t a_row0,
+             const __nv_bfloat16* B, int64_t b_rows, int64_t b_ld, int64_t M, int64_t N, int64_t K,
+             const double* rowscale, const double* colscale, double* out, int64_t ld_out, int* err) {
+  plane_gemm<Exact6>(c, z, A, a_rows, a_ld, a_row0, B, b_rows, b_ld, M, N, K, rowscale, colscale, out, ld_out, err);
 }
 
 // Split-FP16 planes of bra rows (j, a) over nu (the W-generation / XC A-or-B operand) only.
@@ -1325,6 +1229,16 @@ void lp_slice_rows(cphf_ctx* c, const float* src, int64_t rows, int64_t K, int64
                    int* e_out) {
   ProfScope ps_slice(c, PROF_SLICE, 0.0, 4.0 * rows * K + 4.0 * rows * ld);
   slice_rows_kernel<Split2, float><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(
+      src, rows, K, 0, rs, 0, 1, dst, ld, rows * ld, e_out);
+  count_launch();
+  CPHF_CUDA(cudaGetLastError());
+}
+
+// Exact BF16 slice planes [t][r][ld] of FP64 rows r (K elements each, row stride rs), exponents to e_out.
+void oz_slice_rows(cphf_ctx* c, const double* src, int64_t rows, int64_t K, int64_t rs, __nv_bfloat16* dst,
+                   int64_t ld, int* e_out) {
+  ProfScope ps_slice(c, PROF_SLICE, 0.0, 8.0 * rows * K + 2.0 * S * rows * ld);
+  slice_rows_kernel<Exact6, double><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(
       src, rows, K, 0, rs, 0, 1, dst, ld, rows * ld, e_out);
   count_launch();
   CPHF_CUDA(cudaGetLastError());

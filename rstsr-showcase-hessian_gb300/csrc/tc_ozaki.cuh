@@ -3,6 +3,7 @@
 // (src/ri_jk/hess_r.rs:159-176), ~1e-10 relative to sum |A||B| per contraction, for the FP64
 // residual of the mixed-precision solve.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
 #include <cstdint>
@@ -45,5 +46,15 @@ void lp_slice_braw(cphf_ctx* c, OzState& z, int s, const float* bra, int64_t nb)
 // split-FP16 planes [t][r][ld] of FP32 rows r (K elements each, row stride rs); row exponents to e_out
 void lp_slice_rows(cphf_ctx* c, const float* src, int64_t rows, int64_t K, int64_t rs, __half* dst, int64_t ld,
                    int* e_out);
+
+// The same contraction on exact BF16 slice planes (six per operand, 21 products, FP64 out,
+// K ranges of at most 3072 per CTA so that the leading groups accumulate exactly); row and
+// column scales are 2^e of the slicing exponents.
+void oz_gemm(cphf_ctx* c, OzState& z, const __nv_bfloat16* A, int64_t a_rows, int64_t a_ld, int64_t a_row0,
+             const __nv_bfloat16* B, int64_t b_rows, int64_t b_ld, int64_t M, int64_t N, int64_t K,
+             const double* rowscale, const double* colscale, double* out, int64_t ld_out, int* err);
+// exact BF16 slice planes [t][r][ld] of FP64 rows r (K elements each, row stride rs); exponents to e_out
+void oz_slice_rows(cphf_ctx* c, const double* src, int64_t rows, int64_t K, int64_t rs, __nv_bfloat16* dst,
+                   int64_t ld, int* e_out);
 
 }  // namespace cphf

@@ -19,6 +19,7 @@
 #include "ctx.cuh"
 #include "kernels.cuh"
 #include "xc_grouped.cuh"
+#include "xc_tc.cuh"
 
 namespace cphf {
 
@@ -46,6 +47,10 @@ void xc_prepare(cphf_ctx* c) {
 
 void xc_response_fp64(cphf_ctx* c, const double* const* bra, int64_t nb, double* const* out,
                       bool accumulate) {
+  if (c->oz_xc && c->lowp) {
+    xc_response_tc64(c, bra, nb, out, accumulate);
+    return;
+  }
   const double* aobra[2] = {c->spin[0].aobra.as<double>(), c->nspin > 1 ? c->spin[1].aobra.as<double>() : nullptr};
   xc_response_grouped<double>(c, bra, nb, out, accumulate, c->phi.as<double>(), aobra, c->s_ket, c->s_rho);
 }
