@@ -225,21 +225,6 @@ def measure_fp64_peak():
     return 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12
 
 
-def xc_dense_factor(s):
-    """nao * ngrids over the stored (block-sparse) AO values of the grid batches: the extra
-    work of the dense-AO tensor-core XC contractions."""
-    g = s.grid
-    if g is None:
-        return 1.0
-    off = np.asarray(g.atom_offsets)
-    nnz = 0
-    for a in range(len(off) - 1):
-        nz = np.flatnonzero(np.any(g.ao[off[a]:off[a + 1]] != 0, axis=0))
-        if nz.size:
-            nnz += int(off[a + 1] - off[a]) * int(nz[-1] - nz[0] + 1)
-    return s.nao * g.ao.shape[0] / max(nnz, 1)
-
-
 def load_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -386,8 +371,8 @@ def run_gpu(args, world, rank, local):
         "wgen_tcgen05_f16x3": "FP16 hi/lo, the tensor pipe executes 3 split products",
         "term2_tcgen05_f16x3": "FP16 hi/lo, the tensor pipe executes 3 split products",
         "kterm_tcgen05_bf16x6_exact": "exact BF16 slices, the tensor pipe executes 21 slice products",
-        "xc_tcgen05_f16x3": "dense-AO phi (FLOPs counted block-sparse), FP16 hi/lo, 3 split products",
-        "xc_tcgen05_bf16x6_exact": "dense-AO phi (FLOPs counted block-sparse), exact BF16 slices, 21 products",
+        "xc_tcgen05_f16x3": "per grid batch over its AO window, FP16 hi/lo, 3 split products",
+        "xc_tcgen05_bf16x6_exact": "per grid batch over its AO window, exact BF16 slices, 21 slice products",
     }
     if dom_name == "slice_scale_split":
         roof = dict(bound="hbm", achieved=dom["bytes"] / dom["ms"] / 1e6, peak=hbm, unit="GB/s",
@@ -413,10 +398,9 @@ def run_gpu(args, world, rank, local):
         roof.update(bound="fp64 pipe" if dom_name.endswith("fp64") else "fp32 pipe", peak=None,
                     peak_source="SIMT GEMM (no tensor-core form); see the per-class TFLOP/s")
     # products the tensor pipe executes per algorithmic FLOP (slices x slices kept)
-    dense = xc_dense_factor(s) if dom_name.startswith("xc_tcgen05") else 1.0
     products = {"kterm_tcgen05_f16x3": 3, "tgen_tcgen05_f16x3": 3, "wgen_tcgen05_f16x3": 3,
                 "term2_tcgen05_f16x3": 3, "kterm_tcgen05_bf16x6_exact": 21,
-                "xc_tcgen05_f16x3": 3 * dense, "xc_tcgen05_bf16x6_exact": 21 * dense}.get(dom_name)
+                "xc_tcgen05_f16x3": 3, "xc_tcgen05_bf16x6_exact": 21}.get(dom_name)
     if products and roof.get("peak"):
         roof.update(tensor_executed_tflops=roof["achieved"] * products,
                     tensor_executed_frac=roof["achieved"] * products / roof["peak"])

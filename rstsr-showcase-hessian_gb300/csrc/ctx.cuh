@@ -36,12 +36,24 @@ struct OzState {
 };
 
 // Dense split-FP16 forms of phi for the tensor-core XC response (xc_tc.cu).
+// One grid batch of the tensor-core XC response: its points [g0, g0 + npts) and AO window
+// [lo, lo + nwin), the window start rounded down to 8 AOs (lo8, so that the TMA K offset of bra
+// is 16-byte aligned) and its length from there (kw), its first row of the phi^T planes (rT)
+// and its first column in the 8-padded point layout of the q planes (gofs).
+struct XcTcBatch {
+  int64_t g0, npts, lo, nwin, phi_off, lo8, kw, rT, gofs;
+};
+
+// Block-sparse operand planes of phi for the tensor-core XC response (xc_tc.cu).
 struct XcTcState {
-  DevBuf batches, pt_batch;   // batch records and the batch of every grid point
-  DevBuf phiA, phiA_scale;    // [2][ngrids][ldk] planes of phi rows p, scale per point
-  DevBuf phiT, phiT_scale;    // per chunk: [2][nao][ldq] planes of phi^T, scale per AO
+  std::vector<XcTcBatch> hb;  // host copy of the batch records (one more entry: gofs of the end)
+  int64_t ldw = 0, ldpT = 0, nrowT = 0;
+  DevBuf batches, pt_batch, rowmap, colmap;  // records, point -> batch, phi^T row -> batch, q column -> point
+  DevBuf phiB, phiB_scale;    // [t][p][ldw]: phi[p, lo8 + k] over the window of p's batch, scale per point
+  DevBuf phiT, phiT_scale;    // [t][rT + m][ldpT]: phi[g0 + k, lo + m] per batch, scale per row
   DevBuf bpl[2], eb[2], bscale[2];  // planes of bra rows (i, a) per spin, their exponents and scales
-  DevBuf qpl, eq, qscale;
+  DevBuf v, qpl, qscale;      // w f rho1 of a chunk and spin, planes of q rows (i, a), their scales
+  DevBuf qmax;                // column maxima of v and aobra (the split-FP16 q scales)
   bool ready = false;
 };
 

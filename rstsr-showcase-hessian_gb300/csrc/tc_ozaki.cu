@@ -63,14 +63,15 @@ using namespace tcx;
 constexpr int BM = 128, BK = 32;
 constexpr int KMAX = 3072;         // exactness bound of the K range of one CTA
 constexpr int KB_PER_CTA = KMAX / BK;
+constexpr int SHORT_STAGES = 3;    // split-FP16 stages for K ranges of a few blocks (two CTAs per SM)
 
 constexpr int S = Exact6::S;
 
-template <class PR, int BN>
+template <class PR, int BN, int ST = PR::STAGES>
 struct Cfg {
   static constexpr int A_TILE = BM * BK * 2;                 // 8 KB
   static constexpr int B_TILE = BN * BK * 2;                 // 8 / 4 KB
-  static constexpr int STAGES = PR::STAGES;
+  static constexpr int STAGES = ST;
   static constexpr int STAGE_BYTES = PR::S * (A_TILE + B_TILE);
   static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*barriers*/ + 1024 /*alignment*/;
   static_assert(BN == 64 || BN == 128, "tile width");
@@ -87,6 +88,14 @@ struct OzArgs {
   int a_off, b_off;         // depth offset of the chunk's aux function 0
   int a_per_p;              // A depth advances with the aux function
   int a_row0;               // split mode: first A row of the contraction (A rows need no alignment)
+  int b_k0;                 // split mode: K offset of B (elements, a multiple of 16 bytes)
+  int store;                // split mode with one K range per tile: store instead of accumulating
+  // split-FP16 split mode, rho1 epilogue (when rho is set): instead of out, accumulate
+  // rho[m + ld_rho a] += sum_i value[m, n = i + rho_nocc a] ao[m + ld_ao i]
+  float* rho;
+  const float* rho_ao;
+  int64_t ld_rho, ld_ao;
+  int rho_nocc;
   int np, p_per_cta;        // batched: aux functions of the launch, per CTA
   int kb_per_cta;           // split: K blocks per CTA (<= KMAX / BK, the exactness bound)
   // batched split-FP16 T generation writing the FP16 hi / lo planes of T * (*tscale) for
@@ -123,11 +132,13 @@ __device__ __forceinline__ void combine4(float a0, float a1, float a2, float a3,
   lo = e - (hi - s);
 }
 
-// Split-K contractions (terms 1 and 2): one CTA per (tile, K range of at most KMAX).
-template <class PR, int BN>
+// Split-K contractions (terms 1 and 2): one CTA per (tile, K range of at most KMAX).  ST
+// pipeline stages (fewer for short K ranges, so that two CTAs share an SM and one's epilogue
+// overlaps the other's MMAs).
+template <class PR, int BN, int ST = PR::STAGES>
 __global__ void __launch_bounds__(128, 1)
     tc_slice_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB, OzArgs args) {
-  using C = Cfg<PR, BN>;
+  using C = Cfg<PR, BN, ST>;
   constexpr int STAGES = C::STAGES;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -177,7 +188,7 @@ __global__ void __launch_bounds__(128, 1)
 #pragma unroll
         for (int t = 0; t < PR::S; ++t) {
           tma_load_3d(st + t * C::A_TILE, &mA, full, k0, m0 + args.a_row0, t * args.a_depth + da);
-          tma_load_3d(st + PR::S * C::A_TILE + t * C::B_TILE, &mB, full, k0, n0, t * args.b_depth + db);
+          tma_load_3d(st + PR::S * C::A_TILE + t * C::B_TILE, &mB, full, k0 + args.b_k0, n0, t * args.b_depth + db);
         }
       }
       for (int it = max(0, issued - STAGES); it < issued; ++it)
@@ -227,6 +238,17 @@ __global__ void __launch_bounds__(128, 1)
       const bool row_ok = row < args.M;
       const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
       const double rs = row_ok ? args.rowscale[row] : 0.0;
+      // rho1 epilogue state: orbital i and right-hand side a of column n0, partial sum
+      int rho_i = 0, rho_a = 0;
+      float rho_acc = 0.f;
+      const float* rho_ao_row = nullptr;
+      if constexpr (PR::NACC == 1) {
+        if (args.rho != nullptr) {
+          rho_i = n0 % args.rho_nocc;
+          rho_a = n0 / args.rho_nocc;
+          rho_ao_row = args.rho_ao + (row_ok ? row : 0);
+        }
+      }
       for (int c = 0; c < BN / 32; ++c) {
         if constexpr (PR::NACC == 4) {
           float v0[32], v1[32], v2[32], v3[32];
@@ -242,23 +264,46 @@ __global__ void __launch_bounds__(128, 1)
                 float hi, lo;
                 combine4(v0[j], v1[j], v2[j], v3[j], hi, lo);
                 const double v = ((double)hi + (double)lo) * (rs * args.colscale[n]);
-                atomicAdd(reinterpret_cast<double*>(args.out) + row + args.ld_out * (int64_t)n, v);
+                double* o = reinterpret_cast<double*>(args.out) + row + args.ld_out * (int64_t)n;
+                if (args.store) *o = v;
+                else atomicAdd(o, v);
               }
             }
           }
         } else {
           float v[32];
           tmem_ld32(lane_base + (uint32_t)(c * 32), v);
-          if (row_ok) {
+          if (row_ok && args.rho != nullptr) {
+            // rho1 of this row: columns n = i + nocc a, the running i / a carried across chunks
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
               const int n = n0 + c * 32 + j;
-              if (n < args.N)
-                atomicAdd(reinterpret_cast<float*>(args.out) + row + args.ld_out * (int64_t)n,
-                          v[j] * (float)(rs * args.colscale[n]));
+              if (n < args.N) {
+                rho_acc += v[j] * (float)(rs * args.colscale[n]) * rho_ao_row[args.ld_ao * (int64_t)rho_i];
+                if (++rho_i == args.rho_nocc) {
+                  atomicAdd(args.rho + row + args.ld_rho * (int64_t)rho_a, rho_acc);
+                  rho_acc = 0.f;
+                  rho_i = 0;
+                  ++rho_a;
+                }
+              }
+            }
+          } else if (row_ok) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              const int n = n0 + c * 32 + j;
+              if (n < args.N) {
+                float* o = reinterpret_cast<float*>(args.out) + row + args.ld_out * (int64_t)n;
+                const float x = v[j] * (float)(rs * args.colscale[n]);
+                if (args.store) *o = x;
+                else atomicAdd(o, x);
+              }
             }
           }
         }
+      }
+      if constexpr (PR::NACC == 1) {
+        if (row_ok && args.rho != nullptr && rho_i > 0) atomicAdd(args.rho + row + args.ld_rho * (int64_t)rho_a, rho_acc);
       }
     }
   }
@@ -655,9 +700,20 @@ CUtensorMap make_map(const void* base, int64_t K, int64_t rows, int64_t depth, i
 }
 
 template <class PR, int BN>
+bool set_short_smem_attr() {
+  if constexpr (PR::S == 6) {
+    return true;
+  } else {
+    return cudaFuncSetAttribute(tc_slice_kernel<PR, BN, SHORT_STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                Cfg<PR, BN, SHORT_STAGES>::SMEM_BYTES) == cudaSuccess;
+  }
+}
+
+template <class PR, int BN>
 bool set_smem_attr() {
   return cudaFuncSetAttribute(tc_slice_kernel<PR, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               Cfg<PR, BN>::SMEM_BYTES) == cudaSuccess &&
+         set_short_smem_attr<PR, BN>() &&
          cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               Batched<PR>::SMEM_BYTES) == cudaSuccess &&
          (PR::S == 6 ||
@@ -718,12 +774,12 @@ float time_launch(cudaStream_t s, F&& launch) {
 }
 
 // split-K contraction: grid (tiles, K ranges)
-template <class PR, int BN>
+template <class PR, int BN, int ST = PR::STAGES>
 void launch_split_raw(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, const OzArgs& a) {
   const unsigned tiles = (unsigned)(a.m_tiles * div_up(a.N, BN));
   const int64_t ranges = div_up(a.total_kb, a.kb_per_cta);
   if (ranges > 65535) throw Error(CPHF_ERR_ARG, "tensor-core K term: grid too large");
-  tc_slice_kernel<PR, BN><<<dim3(tiles, (unsigned)ranges), 128, Cfg<PR, BN>::SMEM_BYTES, c->stream>>>(mA, mB, a);
+  tc_slice_kernel<PR, BN, ST><<<dim3(tiles, (unsigned)ranges), 128, Cfg<PR, BN, ST>::SMEM_BYTES, c->stream>>>(mA, mB, a);
   count_launch();
   CPHF_CUDA(cudaGetLastError());
 }
@@ -1178,12 +1234,13 @@ void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t
 // over FP16 hi / lo planes (plane stride rows x ld elements), K-major, FP32 atomics into out
 // [m + ld_out n]; the K range is split over CTAs as the autotuner finds best.
 template <class PR, class TOut>
-void plane_gemm(cphf_ctx* c, OzState& z, const typename PR::Elem* A, int64_t a_rows, int64_t a_ld, int64_t a_row0,
-                const typename PR::Elem* B, int64_t b_rows, int64_t b_ld, int64_t M, int64_t N, int64_t K,
-                const double* rowscale, const double* colscale, TOut* out, int64_t ld_out, int* err) {
+void plane_gemm(cphf_ctx* c, OzState& z, const PlaneMat& A, int64_t a_row0, const PlaneMat& B, int64_t b_k0,
+                int64_t M, int64_t N, int64_t K, const double* rowscale, const double* colscale, TOut* out,
+                int64_t ld_out, int* err, int kb_per_cta, bool store, const RhoEpilogue* rho = nullptr) {
   if (M <= 0 || N <= 0 || K <= 0) return;
-  const CUtensorMap mA = make_map(A, K, a_rows, PR::S, a_ld, BM, PR::BF16);
-  const CUtensorMap mB = make_map(B, K, b_rows, PR::S, b_ld, BM, PR::BF16);
+  if (b_k0 % 8 != 0 || b_k0 < 0) throw Error(CPHF_ERR_ARG, "tensor-core contraction: B offset not 16-byte aligned");
+  const CUtensorMap mA = make_map(A.p, A.kext, A.rows, PR::S, A.ld, BM, PR::BF16);
+  const CUtensorMap mB = make_map(B.p, B.kext, B.rows, PR::S, B.ld, BM, PR::BF16);
   OzArgs a = base_args(z, (int)M, (int)N);
   a.err = err;
   a.out = out;
@@ -1192,22 +1249,51 @@ void plane_gemm(cphf_ctx* c, OzState& z, const typename PR::Elem* A, int64_t a_r
   a.a_depth = 1;
   a.b_depth = 1;
   a.a_row0 = (int)a_row0;
+  a.b_k0 = (int)b_k0;
   a.rowscale = rowscale;
   a.colscale = colscale;
   a.ld_out = ld_out;
-  launch_split<PR, 128>(c, z, mA, mB, a);
+  if (rho != nullptr) {
+    if (PR::NACC != 1 || rho->nocc <= 0) throw Error(CPHF_ERR_ARG, "rho1 epilogue: split-FP16 contractions only");
+    a.rho = rho->rho;
+    a.rho_ao = rho->ao;
+    a.ld_rho = rho->ld_rho;
+    a.ld_ao = rho->ld_ao;
+    a.rho_nocc = (int)rho->nocc;
+  }
+  if (kb_per_cta > 0) {
+    a.kb_per_cta = PR::NACC == 4 ? std::min(kb_per_cta, KB_PER_CTA) : kb_per_cta;
+    a.store = store && a.kb_per_cta >= a.total_kb;
+    bool launched = false;
+    if constexpr (PR::NACC == 1) {
+      if (a.kb_per_cta <= 2 * SHORT_STAGES) {
+        launch_split_raw<PR, 128, SHORT_STAGES>(c, mA, mB, a);
+        launched = true;
+      }
+    }
+    if (!launched) launch_split_raw<PR, 128>(c, mA, mB, a);
+  } else {
+    launch_split<PR, 128>(c, z, mA, mB, a);
+  }
 }
 
-void lp_gemm(cphf_ctx* c, OzState& z, const __half* A, int64_t a_rows, int64_t a_ld, int64_t a_row0,
-             const __half* B, int64_t b_rows, int64_t b_ld, int64_t M, int64_t N, int64_t K,
-             const double* rowscale, const double* colscale, float* out, int64_t ld_out, int* err) {
-  plane_gemm<Split2>(c, z, A, a_rows, a_ld, a_row0, B, b_rows, b_ld, M, N, K, rowscale, colscale, out, ld_out, err);
+void lp_gemm(cphf_ctx* c, OzState& z, const PlaneMat& A, int64_t a_row0, const PlaneMat& B, int64_t b_k0, int64_t M,
+             int64_t N, int64_t K, const double* rowscale, const double* colscale, float* out, int64_t ld_out,
+             int* err, int kb_per_cta, bool store) {
+  plane_gemm<Split2>(c, z, A, a_row0, B, b_k0, M, N, K, rowscale, colscale, out, ld_out, err, kb_per_cta, store);
 }
 
-void oz_gemm(cphf_ctx* c, OzState& z, const __nv_bfloat16* A, int64_t a_rows, int64_t a_ld, int64_t a_row0,
-             const __nv_bfloat16* B, int64_t b_rows, int64_t b_ld, int64_t M, int64_t N, int64_t K,
-             const double* rowscale, const double* colscale, double* out, int64_t ld_out, int* err) {
-  plane_gemm<Exact6>(c, z, A, a_rows, a_ld, a_row0, B, b_rows, b_ld, M, N, K, rowscale, colscale, out, ld_out, err);
+void lp_gemm_rho(cphf_ctx* c, OzState& z, const PlaneMat& A, int64_t a_row0, const PlaneMat& B, int64_t b_k0,
+                 int64_t M, int64_t N, int64_t K, const double* rowscale, const double* colscale,
+                 const RhoEpilogue& rho, int* err, int kb_per_cta) {
+  plane_gemm<Split2>(c, z, A, a_row0, B, b_k0, M, N, K, rowscale, colscale, (float*)nullptr, 0, err, kb_per_cta, false,
+                     &rho);
+}
+
+void oz_gemm(cphf_ctx* c, OzState& z, const PlaneMat& A, int64_t a_row0, const PlaneMat& B, int64_t b_k0, int64_t M,
+             int64_t N, int64_t K, const double* rowscale, const double* colscale, double* out, int64_t ld_out,
+             int* err, int kb_per_cta, bool store) {
+  plane_gemm<Exact6>(c, z, A, a_row0, B, b_k0, M, N, K, rowscale, colscale, out, ld_out, err, kb_per_cta, store);
 }
 
 // Split-FP16 planes of bra rows (j, a) over nu (the W-generation / XC A-or-B operand) only.

@@ -34,12 +34,21 @@ void lp_tgen_planes(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int
 void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, double alpha, float* out,
                 int* err);
 
-// Split-FP16 contraction out[m, n] += rowscale[m] colscale[n] sum_k A[a_row0 + m, k] B[n, k]:
-// A, B FP16 hi / lo planes (K-major rows of ld elements; lo plane rows x ld elements after hi),
-// out FP32 [m + ld_out n] accumulated with atomics.
-void lp_gemm(cphf_ctx* c, OzState& z, const __half* A, int64_t a_rows, int64_t a_ld, int64_t a_row0,
-             const __half* B, int64_t b_rows, int64_t b_ld, int64_t M, int64_t N, int64_t K,
-             const double* rowscale, const double* colscale, float* out, int64_t ld_out, int* err);
+// A stack of operand planes: plane t holds rows x ld elements at p + t rows ld; columns at
+// and beyond kext read as zero (as do rows beyond `rows`).
+struct PlaneMat {
+  const void* p;
+  int64_t rows, ld, kext;
+};
+
+// Split-FP16 contraction (hi / lo planes, three products, FP32 accumulation)
+//   out[m + ld_out n] += rowscale[m] colscale[n] sum_{k < K} A[a_row0 + m, k] B[n, b_k0 + k]
+// with FP32 atomics; b_k0 a multiple of 8.  The K range is split over CTAs in ranges of
+// kb_per_cta blocks of 32 (0: as the autotuner finds best); with store and one range per
+// tile the values are stored, not accumulated.
+void lp_gemm(cphf_ctx* c, OzState& z, const PlaneMat& A, int64_t a_row0, const PlaneMat& B, int64_t b_k0, int64_t M,
+             int64_t N, int64_t K, const double* rowscale, const double* colscale, float* out, int64_t ld_out,
+             int* err, int kb_per_cta = 0, bool store = false);
 
 // split-FP16 planes of bra's rows (j, a) over nu into z.braw (exponents z.ebraw) only
 void lp_slice_braw(cphf_ctx* c, OzState& z, int s, const float* bra, int64_t nb);
@@ -47,12 +56,24 @@ void lp_slice_braw(cphf_ctx* c, OzState& z, int s, const float* bra, int64_t nb)
 void lp_slice_rows(cphf_ctx* c, const float* src, int64_t rows, int64_t K, int64_t rs, __half* dst, int64_t ld,
                    int* e_out);
 
+// The same contraction reduced to rho1 in its epilogue (the XC response's first grid step):
+//   rho[m + ld_rho a] += sum_i ao[m + ld_ao i] sum_k A[a_row0 + m, k] B[n = i + nocc a, b_k0 + k]
+// (rowscale / colscale applied as above; rho FP32, accumulated with atomics).
+struct RhoEpilogue {
+  float* rho;
+  const float* ao;
+  int64_t ld_rho, ld_ao, nocc;
+};
+void lp_gemm_rho(cphf_ctx* c, OzState& z, const PlaneMat& A, int64_t a_row0, const PlaneMat& B, int64_t b_k0,
+                 int64_t M, int64_t N, int64_t K, const double* rowscale, const double* colscale,
+                 const RhoEpilogue& rho, int* err, int kb_per_cta);
+
 // The same contraction on exact BF16 slice planes (six per operand, 21 products, FP64 out,
 // K ranges of at most 3072 per CTA so that the leading groups accumulate exactly); row and
 // column scales are 2^e of the slicing exponents.
-void oz_gemm(cphf_ctx* c, OzState& z, const __nv_bfloat16* A, int64_t a_rows, int64_t a_ld, int64_t a_row0,
-             const __nv_bfloat16* B, int64_t b_rows, int64_t b_ld, int64_t M, int64_t N, int64_t K,
-             const double* rowscale, const double* colscale, double* out, int64_t ld_out, int* err);
+void oz_gemm(cphf_ctx* c, OzState& z, const PlaneMat& A, int64_t a_row0, const PlaneMat& B, int64_t b_k0, int64_t M,
+             int64_t N, int64_t K, const double* rowscale, const double* colscale, double* out, int64_t ld_out,
+             int* err, int kb_per_cta = 0, bool store = false);
 // exact BF16 slice planes [t][r][ld] of FP64 rows r (K elements each, row stride rs); exponents to e_out
 void oz_slice_rows(cphf_ctx* c, const double* src, int64_t rows, int64_t K, int64_t rs, __nv_bfloat16* dst,
                    int64_t ld, int* e_out);
