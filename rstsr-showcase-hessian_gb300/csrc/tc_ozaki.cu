@@ -238,6 +238,7 @@ __global__ void __launch_bounds__(128, 1)
       const bool row_ok = row < args.M;
       const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
       const double rs = row_ok ? args.rowscale[row] : 0.0;
+      const float rsf = (float)rs;
       // rho1 epilogue state: orbital i and right-hand side a of column n0, partial sum
       int rho_i = 0, rho_a = 0;
       float rho_acc = 0.f;
@@ -273,13 +274,23 @@ __global__ void __launch_bounds__(128, 1)
         } else {
           float v[32];
           tmem_ld32(lane_base + (uint32_t)(c * 32), v);
+          // the chunk's 32 column scales: one load per lane, broadcast by shuffles (no FP64 per
+          // element); rowscale and colscale are powers of two (times a small factor), so the
+          // FP32 product equals the FP64 one
+          float cs[32];
+          {
+            const int nl = n0 + c * 32 + lane;
+            const float csl = nl < args.N ? (float)args.colscale[nl] : 0.f;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) cs[j] = __shfl_sync(0xffffffffu, csl, j) * rsf;
+          }
           if (row_ok && args.rho != nullptr) {
             // rho1 of this row: columns n = i + nocc a, the running i / a carried across chunks
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
               const int n = n0 + c * 32 + j;
               if (n < args.N) {
-                rho_acc += v[j] * (float)(rs * args.colscale[n]) * rho_ao_row[args.ld_ao * (int64_t)rho_i];
+                rho_acc += v[j] * cs[j] * rho_ao_row[args.ld_ao * (int64_t)rho_i];
                 if (++rho_i == args.rho_nocc) {
                   atomicAdd(args.rho + row + args.ld_rho * (int64_t)rho_a, rho_acc);
                   rho_acc = 0.f;
@@ -294,7 +305,7 @@ __global__ void __launch_bounds__(128, 1)
               const int n = n0 + c * 32 + j;
               if (n < args.N) {
                 float* o = reinterpret_cast<float*>(args.out) + row + args.ld_out * (int64_t)n;
-                const float x = v[j] * (float)(rs * args.colscale[n]);
+                const float x = v[j] * cs[j];
                 if (args.store) *o = x;
                 else atomicAdd(o, x);
               }
