@@ -69,9 +69,10 @@ typedef struct cphf_config {
   int64_t xc_chunk_points;   /* grid points per XC chunk (default 0 = 8 GiB of intermediates) */
   int32_t residual_dfloat;   /* mixed: arithmetic of the correction residuals.  0 = native FP64;
                                 1 = double-float GEMMs on the FP32 pipes (~1e-14 relative);
-                                2 = as 1, with the whole RI-K term on the tensor cores as exact BF16
-                                slice products (6 x 6 bits, ~1e-10 relative to the operand row maxima;
-                                default; without tensor cores it behaves as 1).
+                                2 = as 1, with the whole RI-K term and the XC grid contractions on the
+                                tensor cores as exact BF16 slice products (6 x 6 bits, ~1e-10 relative
+                                to the operand row maxima; default; without tensor cores it behaves
+                                as 1).
                                 The final verification (verify_residual) is always native FP64. */
   int32_t cuda_graphs;       /* mixed: replay each block width's split-precision operator application
                                 from a captured CUDA graph (default 1); bypassed while profiling */
