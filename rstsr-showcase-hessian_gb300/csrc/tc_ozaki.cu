@@ -285,12 +285,23 @@ __global__ void __launch_bounds__(128, 1)
             for (int j = 0; j < 32; ++j) cs[j] = __shfl_sync(0xffffffffu, csl, j) * rsf;
           }
           if (row_ok && args.rho != nullptr) {
-            // rho1 of this row: columns n = i + nocc a, the running i / a carried across chunks
+            // rho1 of this row: columns n = i + nocc a, the running i / a carried across chunks.
+            // The chunk's 32 ao values are loaded first, back to back (independent L2 loads),
+            // then reduced.
+            float aov[32];
+            {
+              int ii = rho_i;
+#pragma unroll
+              for (int j = 0; j < 32; ++j) {
+                aov[j] = n0 + c * 32 + j < args.N ? rho_ao_row[args.ld_ao * (int64_t)ii] : 0.f;
+                if (++ii == args.rho_nocc) ii = 0;
+              }
+            }
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
               const int n = n0 + c * 32 + j;
               if (n < args.N) {
-                rho_acc += v[j] * cs[j] * rho_ao_row[args.ld_ao * (int64_t)rho_i];
+                rho_acc += v[j] * cs[j] * aov[j];
                 if (++rho_i == args.rho_nocc) {
                   atomicAdd(args.rho + row + args.ld_rho * (int64_t)rho_a, rho_acc);
                   rho_acc = 0.f;
@@ -1305,20 +1316,6 @@ void oz_gemm(cphf_ctx* c, OzState& z, const PlaneMat& A, int64_t a_row0, const P
              int64_t N, int64_t K, const double* rowscale, const double* colscale, double* out, int64_t ld_out,
              int* err, int kb_per_cta, bool store) {
   plane_gemm<Exact6>(c, z, A, a_row0, B, b_k0, M, N, K, rowscale, colscale, out, ld_out, err, kb_per_cta, store);
-}
-
-// Split-FP16 planes of bra rows (j, a) over nu (the W-generation / XC A-or-B operand) only.
-void lp_slice_braw(cphf_ctx* c, OzState& z, int s, const float* bra, int64_t nb) {
-  const int64_t nao = c->nao, no = c->spin[s].nocc, N = no * nb;
-  z.ldk = (nao + 7) / 8 * 8;
-  const int64_t ldk = z.ldk;
-  z.braw.ensure((size_t)Split2::S * N * ldk * 2, c->counter());
-  z.ebraw.ensure((size_t)N * 4, c->counter());
-  ProfScope ps_slice(c, PROF_SLICE, 0.0, 8.0 * N * nao + 4.0 * N * ldk);
-  slice_rows_kernel<Split2, float><<<grid_warps(N, c->num_sms), 256, 0, c->stream>>>(
-      bra, N, nao, 0, nao, 0, 1, z.braw.as<__half>(), ldk, N * ldk, z.ebraw.as<int>());
-  count_launch();
-  CPHF_CUDA(cudaGetLastError());
 }
 
 // Split-FP16 planes [t][r][ld] of FP32 rows r (K elements each, row stride rs), exponents to e_out.

@@ -50,8 +50,6 @@ void lp_gemm(cphf_ctx* c, OzState& z, const PlaneMat& A, int64_t a_row0, const P
              int64_t N, int64_t K, const double* rowscale, const double* colscale, float* out, int64_t ld_out,
              int* err, int kb_per_cta = 0, bool store = false);
 
-// split-FP16 planes of bra's rows (j, a) over nu into z.braw (exponents z.ebraw) only
-void lp_slice_braw(cphf_ctx* c, OzState& z, int s, const float* bra, int64_t nb);
 // split-FP16 planes [t][r][ld] of FP32 rows r (K elements each, row stride rs); row exponents to e_out
 void lp_slice_rows(cphf_ctx* c, const float* src, int64_t rows, int64_t K, int64_t rs, __half* dst, int64_t ld,
                    int* e_out);
