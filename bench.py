@@ -416,7 +416,7 @@ def run_gpu(args, world, rank, local):
         ms_per_step=t_step * 1e3, higher_is_better=False, scaling="weak", vs_baseline=None,
         dtype=("f16x3 tensor-core operator / f32 / f64 defect correction"
                + {0: " (fp64 residual)", 1: " (double-float residual)",
-                  2: " (residual: bf16x6 exact-slice tensor-core K term + double-float)"}[args.residual]),
+                  2: " (residual: bf16x6 exact-slice tensor-core K term and XC + double-float)"}[args.residual]),
         data=f"synthetic (seeded generator, {args.workload}, seed {args.seed})",
         config=dict(workload=args.workload, description=WORKLOAD_DESC.get(args.workload, args.workload),
                     precision="mixed", learned_guess=learned, residual_mode=args.residual,
