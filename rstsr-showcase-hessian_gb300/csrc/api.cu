@@ -479,7 +479,7 @@ cphf_status cphf_solve_dimless_cphf(cphf_ctx* c, const double* const* rhs, int64
     check_finite(c, b, n * nprop, "rhs");
     if (x0) pack_krylov(c, x0, nprop, xg);
     const double* x0p = x0 ? xg : nullptr;
-    // learned initial guess and left preconditioner (the unpreconditioned FP64 residual stays the judge)
+    // learned initial guess and left preconditioner (convergence is still decided on the unpreconditioned FP64 residual)
     DevBuf pre;
     double* m = nullptr;
     if (c->cfg.use_learned_guess) {
