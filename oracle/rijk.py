@@ -19,7 +19,10 @@ Shapes follow the reference (col-major semantics, numpy indexing):
 ``cderi [nao_tp, naux]``, ``mo_coeff [nao, nmo]``, ``mo_occ [nmo]``,
 ``bra [nao, nocc, nprop]``.  The per-RHS loop of ``hess_r.rs:164-176`` is
 evaluated as one GEMM over all RHS of an aux batch (same products and sums,
-only the loop order of independent RHS differs).
+only the loop order of independent RHS differs).  Every contraction that the reference
+performs as a matrix product runs through BLAS here too (``tensordot``), so
+that the timed CPU baseline reflects the reference's arithmetic and not numpy's generic
+einsum loop.
 """
 
 import numpy as np
@@ -74,7 +77,7 @@ def rijk_response_bra_separated(cderi, mo_coeff, mo_occ, bra, do_j=True, do_k=Tr
         # hess_r.rs:131-139
         dm1 = np.zeros((nao, nao, nprop))
         for s in range(nset):
-            dm1 += np.einsum("uin,vi->uvn", bra[s], mocc[s])
+            dm1 += np.tensordot(bra[s], mocc[s], axes=([1], [1])).transpose(0, 2, 1)  # uin,vi->uvn
         dm1 = dm1 + dm1.transpose(1, 0, 2)
         dm1_tp = pack_triu_tilde(dm1)
         itm_j_aux = cderi.T @ dm1_tp
@@ -94,8 +97,8 @@ def rijk_response_bra_separated(cderi, mo_coeff, mo_occ, bra, do_j=True, do_k=Tr
                 nb = p1 - p0
                 cd = unpack_tri_sym(cderi[:, p0:p1], nao)            # [mu, nu, P]
                 # hess_r.rs:160-162: bxo[nu,P,i] = sum_mu B[mu,nu,P] C[mu,i]; oxo[k,P,i]
-                bxo = np.einsum("uvP,ui->vPi", cd, mocc_s)
-                oxo = np.einsum("vk,vPi->kPi", mocc_s, bxo)
+                bxo = np.tensordot(cd, mocc_s, axes=([0], [0]))            # uvP,ui->vPi
+                oxo = np.tensordot(mocc_s, bxo, axes=([0], [0]))           # vk,vPi->kPi
                 # hess_r.rs:168: bxo1[nu,P,j,a] = sum_mu B[mu,nu,P] bra[mu,j,a]
                 bxo1 = (cd.reshape(nao, nao * nb).T @ bra_mat).reshape(nao, nb, no, nprop)
                 # hess_r.rs:169-170: resp[nu,k,a] -= sum_{P,j} bxo1[nu,P,j,a] oxo[k,P,j]
@@ -120,7 +123,7 @@ def rhf_response_bra(cderi, mo_coeff, mo_occ, bra, scale_j, scale_k):
     nprop = int(np.prod(shape[2:])) if len(shape) > 2 else 1
     resp = np.zeros((nao, nocc, nprop))
     if j_ao is not None:
-        resp += scale_j * np.einsum("uvn,vi->uin", j_ao, mocc)
+        resp += scale_j * np.tensordot(j_ao, mocc, axes=([1], [0])).transpose(0, 2, 1)  # uvn,vi->uin
     if k_bras:
         resp += scale_k * k_bras[0].reshape(nao, nocc, nprop)
     return resp.reshape(shape)
@@ -138,7 +141,7 @@ def uhf_response_bra(cderi, mo_coeff, mo_occ, bra, scale_j, scale_k):
         nprop = int(np.prod(shape[2:])) if len(shape) > 2 else 1
         r = np.zeros((nao, mocc.shape[1], nprop))
         if j_ao is not None:
-            r += 0.5 * scale_j * np.einsum("uvn,vi->uin", j_ao, mocc)
+            r += 0.5 * scale_j * np.tensordot(j_ao, mocc, axes=([1], [0])).transpose(0, 2, 1)  # uvn,vi->uin
         if k_bras:
             r += scale_k * k_bras[s].reshape(r.shape)
         out.append(r.reshape(shape))
