@@ -19,7 +19,10 @@
 //     points, zero-padded to ldpT, one scale per row;
 //   * GEMM 2's B: q is generated per chunk and spin straight from v and aobra into planes over
 //     8-padded batch segments, so that each batch's K offset is 16-byte aligned.
-// The rho1 step between the GEMMs is the kernel of the SIMT path.
+// Split FP16 reduces GEMM 1 to rho1[p, a] = sum_i aobra[p, i] ket[p, (i, a)] in its epilogue (ket
+// is never written) and generates q's planes in one pass from column-maximum bounds; the exact
+// slices store ket, take rho1 from the SIMT path's kernel and slice q with its exact row maxima
+// (fixed-point slices are relative to the row scale, so a loose bound would cost accuracy).
 #include <algorithm>
 #include <type_traits>
 #include <vector>
