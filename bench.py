@@ -1,14 +1,28 @@
 #!/usr/bin/env python3
 """Benchmark: time to a converged CPHF solve (max_j ||b - (I+A)x||_2 < 1e-8) on one GB300.
 
-A step is one full ``solve_dimless_cphf`` of the workload (default ``rhf_nao600``:
-nao=600, naux=2000, nocc=60, 180 right-hand sides, RHF with RI-J/RI-K response) through
-libcphf.  The timed arm is the mixed-precision solve (split-FP16 tensor-core operator
-inside FP64 defect correction); the plain FP64 GPU solve of the same system is timed once
-beside it, and both solutions are verified with the FP64 operator outside the timed region.
+A step is one full ``solve_dimless_cphf`` of the workload through libcphf.  The default
+workload is ``rhf_nao1200``: RHF with RI-J/RI-K response, nao=1200, naux=4000, nocc=120,
+360 right-hand sides (120 atoms), the size the headline metric is quoted on.  The timed arm is
+the mixed-precision solve with the learned preconditioner (split-FP16 tensor-core operator
+inside defect correction whose every correction residual, the final one included, is
+recomputed with the FP64-accurate exact-slice operator inside the solve).
 
-``--impl reference`` times the reference algorithm on the host CPU instead (the numpy
-port in ``oracle/``, all cores), on the same workload and metric.
+* ``value``: the solve with its inputs resident in HBM (CUDA events on the library stream).
+* ``e2e``: per step, from pinned host buffers through the public API: the packed cderi upload
+  (``set_cderi``), ``make_response_preparation`` (Z/O, the FP16 / BF16 planes of B) and the
+  solve with the right-hand side in and U1 out.
+* ``fp64_plain``: the plain FP64 GPU solve of the same system.  Measured in full where it fits
+  the run (nrhs <= 180); at the larger sizes its operator-call count comes from a measured FP64
+  solve of a column subset and its per-call cost from measured FP64 applications at two widths
+  (the K term is linear in the column count), labelled ``extrapolated``.
+* Accuracy: U1 and the Hessian blocks of the mixed solve against the FP64 solve (all columns
+  where the FP64 solve is measured in full, else the subset's columns and the Hessian blocks
+  of the subset's atoms), and the native FP64 residual of the mixed solution.
+
+``--impl reference`` times the reference algorithm on the host CPU instead (the numpy port in
+``oracle/``, all cores), on bounded samples of the same workload, extrapolated and labelled.
+``--apply-only`` times single operator applications (launch lists and profiler captures).
 
 Prints one JSON line (rank 0).  Multi-GPU runs are independent replicas (the path is not
 sharded): one process per GPU via torchrun, max time over ranks.
@@ -32,39 +46,55 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "time to converged CPHF (||r||<1e-8): mixed+learned vs plain FP64, same GB300"
 WORKLOAD_DESC = {
+    "rhf_nao1200": "RHF CPHF, RI-JK response: nao=1200 naux=4000 nocc=120 nvir=1080 nrhs=360 (120 atoms)",
     "rhf_nao600": "RHF CPHF, RI-JK response: nao=600 naux=2000 nocc=60 nvir=540 nrhs=180 (60 atoms)",
     "rhf_nao24": "RHF CPHF, RI-JK response: nao=24 naux=84 nocc=5 nrhs=12 (4 atoms)",
     "rhf_nao300": "RHF CPHF, RI-JK response: nao=300 naux=1000 nocc=30 nrhs=90 (30 atoms)",
     "rks_nao600": "RKS CPKS, RI-JK + LDA XC response on ~660k grid points: nao=600 naux=2000 nocc=60 nrhs=180",
     "uks_nao800": "UKS CPKS, RI-JK + LDA XC: nao=800 naux=2700 nocc=80/78 nrhs=240",
-    "rhf_nao1200": "RHF CPHF, RI-JK response: nao=1200 naux=4000 nocc=120 nrhs=360",
 }
+FULL_FP64_MAX_NRHS = 180   # above this the plain FP64 solve is extrapolated (config 4: ~2900 s)
 
 
-def parse():
+def parse(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=2)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["cphf", "reference"], default="cphf")
-    p.add_argument("--workload", default="rhf_nao600")
+    p.add_argument("--workload", default="rhf_nao1200")
     p.add_argument("--seed", type=int, default=0)
-    p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison solve")
-    p.add_argument("--cpu-sample", type=int, default=6, help="RHS columns of the CPU baseline sample")
+    p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 leg")
+    p.add_argument("--fp64-full", action="store_true", help="always run the plain FP64 solve in full")
+    p.add_argument("--fp64-cols", type=int, default=6,
+                   help="columns of the measured FP64 subset solve (when the full solve is extrapolated)")
+    p.add_argument("--fp64-app-cols", type=int, default=36,
+                   help="width of the wider measured FP64 application (extrapolation, residual check)")
+    p.add_argument("--e2e-steps", type=int, default=2, help="end-to-end steps (0: as many as --steps)")
+    p.add_argument("--cpu-sample", type=int, default=0, help="RHS columns of the CPU baseline sample (0: auto)")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg (profiling runs)")
     p.add_argument("--inner-tol", type=float, default=None, help="Krylov tol of the inner solves (library default)")
     p.add_argument("--no-graphs", action="store_true", help="run the inner operator eagerly (no CUDA graphs)")
-    p.add_argument("--verify-cols", type=int, default=0,
-                   help="verify the FP64 residual on the first K perturbations only (0: all)")
-    p.add_argument("--no-learned", action="store_true", help="do not use the trained initial guess")
+    p.add_argument("--no-learned", action="store_true", help="do not use the trained network")
+    p.add_argument("--learned-mode", type=int, default=1, choices=[1, 2],
+                   help="1: learned preconditioner; 2: preconditioner and initial guess")
+    p.add_argument("--no-learned-gain", action="store_true", help="skip the solve without the network")
     p.add_argument("--fp64-tol", type=float, default=1e-10, help="Krylov tol of the plain FP64 solve")
     p.add_argument("--fp64-lindep", type=float, default=1e-20,
                    help="Krylov lindep of the plain FP64 solve; the convergence test is max(lindep, tol^2), "
                         "so the default 1e-14 would stop it above the ||r|| < 1e-8 target")
     p.add_argument("--residual", type=int, default=2, choices=[0, 1, 2],
-                   help="mixed solve's correction residual: 0 FP64, 1 double-float, 2 double-float + "
-                        "tensor-core K term with exact BF16 slices")
-    return p.parse_args()
+                   help="mixed solve's correction residuals: 0 FP64, 1 double-float, 2 double-float + "
+                        "tensor-core K term and XC with exact BF16 slices")
+    p.add_argument("--verify", type=int, default=2, choices=[0, 1, 2],
+                   help="mixed solve's final check: 2 recomputed with the --residual operator, 1 native FP64, "
+                        "0 updated with the split-precision operator")
+    p.add_argument("--apply-only", action="store_true",
+                   help="only time --reps operator applications of --nb columns (launch lists / captures)")
+    p.add_argument("--nb", type=int, default=0, help="--apply-only: columns per application (0: all RHS)")
+    p.add_argument("--reps", type=int, default=3, help="--apply-only: applications")
+    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="--apply-only: operator")
+    return p.parse_args(argv)
 
 
 def dist_setup(args):
@@ -122,70 +152,86 @@ def _rhs_cut(s):
     return nrhs, cut
 
 
-def cpu_oracle_calibrate(s, ncols):
-    """Reference algorithm on the host (oracle port): a real Krylov solve of `ncols` RHS
-    columns with the full-size operator gives the operator-call count; single matvecs at
-    ncols and 2*ncols give the per-call cost model t0 + t1*nb."""
+def cpu_sample_cols(s, requested):
+    """RHS columns of one bounded CPU operator sample (about 10-30 s on 16 cores)."""
+    if requested > 0:
+        return requested
+    return 6 if s.nao <= 300 else (2 if s.nao <= 800 else 1)
+
+
+def cpu_oracle_calibrate(s, ncols, wide_cols=0, calls=None):
+    """Reference algorithm on the host (oracle port): the per-call cost model t0 + t1*nb from
+    single operator applications at ncols and 2*ncols columns (and, if wide_cols > 0, one wider
+    application that checks the model); the operator-call count from a real Krylov solve of
+    ncols columns with the full-size operator, unless `calls` (measured elsewhere) is given."""
     drv = cpu_oracle_driver(s)
     nrhs, cut = _rhs_cut(s)
     x1, x2 = cut(ncols), cut(2 * ncols)
     t = time.perf_counter(); drv.response_dimless_cphf(x1); t1 = time.perf_counter() - t
     t = time.perf_counter(); drv.response_dimless_cphf(x2); t2 = time.perf_counter() - t
     slope = max((t2 - t1) / ncols, 1e-12)
-    t = time.perf_counter()
-    drv.solve_dimless_cphf(x1)
-    t_solve = time.perf_counter() - t
-    calls = drv.krylov_stats["aop_calls"]
-    cols_per_call = drv.krylov_stats["aop_columns"] / max(calls, 1) / ncols
-    return dict(drv=drv, nrhs=nrhs, cut=cut, ncols=ncols, t1=t1, t2=t2, slope=slope, t_solve=t_solve,
-                calls=calls, cols_per_call=cols_per_call)
+    cal = dict(drv=drv, nrhs=nrhs, cut=cut, ncols=ncols, t1=t1, t2=t2, slope=slope, t_solve=None,
+               calls=calls, calls_source="given", wide=None)
+    if wide_cols > 0:
+        t = time.perf_counter(); drv.response_dimless_cphf(cut(wide_cols)); tw = time.perf_counter() - t
+        cal["wide"] = (wide_cols, tw, max(t1 - slope * ncols, 0.0) + slope * wide_cols)
+    if calls is None:
+        t = time.perf_counter()
+        drv.solve_dimless_cphf(x1)
+        cal["t_solve"] = time.perf_counter() - t
+        cal["calls"] = drv.krylov_stats["aop_calls"]
+        cal["calls_source"] = f"oracle solve of {ncols} columns"
+    return cal
 
 
 def cpu_oracle_value(cal, t_ncols):
-    """Extrapolated solve time: calls x (t0 + t1 * nrhs * cols_per_call), t0 from a matvec at ncols."""
+    """Extrapolated solve time: calls x (t0 + t1 * nrhs), t0 from an application at ncols."""
     base = max(t_ncols - cal["slope"] * cal["ncols"], 0.0)
-    return cal["calls"] * (base + cal["slope"] * cal["nrhs"] * cal["cols_per_call"])
+    return cal["calls"] * (base + cal["slope"] * cal["nrhs"])
 
 
 def cpu_oracle_record(cal, value):
     cores = os.cpu_count()
     n, nrhs = cal["ncols"], cal["nrhs"]
-    return dict(value=value, unit="s", cores=cores, kind="port",
-                sample=(f"oracle (numpy/OpenBLAS, {cores} threads) CPHF solve of {n} of {nrhs} RHS "
-                        f"({cal['calls']} operator calls, {cal['t_solve']:.1f} s) plus matvecs at {n} and {2 * n} "
-                        f"columns ({cal['t1']:.2f} s, {cal['t2']:.2f} s); value = calls x (t0 + t1*{nrhs}) "
-                        f"extrapolated"),
+    wide = ""
+    if cal["wide"]:
+        w, tw, pred = cal["wide"]
+        wide = f"; check: {w}-column application measured {tw:.1f} s vs model {pred:.1f} s"
+    solve = f", {cal['t_solve']:.1f} s" if cal["t_solve"] is not None else ""
+    return dict(value=value, unit="s", cores=cores, kind="port", extrapolated=True,
+                sample=(f"oracle (numpy/OpenBLAS, {cores} threads): operator applications at {n} and {2 * n} of "
+                        f"{nrhs} RHS columns ({cal['t1']:.2f} s, {cal['t2']:.2f} s) give t0 + t1*nb; "
+                        f"{cal['calls']} operator calls ({cal['calls_source']}{solve}); value = calls x "
+                        f"(t0 + t1*{nrhs}), extrapolated{wide}"),
                 calls=cal["calls"], matvec_s_per_col=cal["slope"])
 
 
-def cpu_oracle_estimate(s, ncols):
-    """One calibration and its extrapolated solve time (the GPU arm's cpu_baseline)."""
-    cal = cpu_oracle_calibrate(s, ncols)
-    return cpu_oracle_record(cal, cpu_oracle_value(cal, cal["t1"]))
-
-
 def run_reference(args, world, rank):
-    """The reference algorithm on the host cores: the call count and per-column cost are
-    calibrated once; every warm-up and timed step is one operator application of the oracle on
-    the sample columns (a bounded sample of the solve), extrapolated to the full solve."""
+    """The reference algorithm on the host cores.  The cost model and call count are calibrated
+    once; every warm-up and timed step is one operator application of the oracle on the sample
+    columns (a bounded sample of the solve), extrapolated to the full solve (labelled)."""
     if rank != 0:
         return
     from cphf_gb300 import synth
     s = synth.make_system(args.workload, seed=args.seed)
-    cal = cpu_oracle_calibrate(s, args.cpu_sample)
+    ncols = cpu_sample_cols(s, args.cpu_sample)
+    wide = 12 if s.nao >= 800 else 3 * s.natm
+    cal = cpu_oracle_calibrate(s, ncols, wide_cols=wide)
     x = cal["cut"](cal["ncols"])
-    values = []
+    values, walls = [], []
     for _ in range(args.warmup + args.steps):
         t = time.perf_counter()
         cal["drv"].response_dimless_cphf(x)
-        values.append(cpu_oracle_value(cal, time.perf_counter() - t))
+        walls.append(time.perf_counter() - t)
+        values.append(cpu_oracle_value(cal, walls[-1]))
     value = statistics.median(values[args.warmup:])
     cb = cpu_oracle_record(cal, value)
     line = dict(metric=METRIC, value=value, unit="s", n_gpus=args.gpus, steps=args.steps, warmup=args.warmup,
                 ms_per_step=value * 1e3, higher_is_better=False, scaling="weak", vs_baseline=None, dtype="f64",
                 data=f"synthetic (seeded generator, {args.workload}, seed {args.seed})",
                 config=dict(workload=args.workload, description=WORKLOAD_DESC.get(args.workload, args.workload)),
-                impl="reference",
+                impl="reference", extrapolated=True,
+                measured_step_s=statistics.median(walls[args.warmup:]),
                 cpu_baseline={k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
                 e2e=dict(value=value, unit="s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
     print(json.dumps(line), flush=True)
@@ -256,8 +302,9 @@ def load_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
-    return 6800.0, 1900.0, "fallback"
+        return (d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0),
+                d.get("bf16_tflops_sustained", d.get("bf16_tflops", 1700.0)), "measured")
+    return 6800.0, 1900.0, 1700.0, "fallback"
 
 
 def fcol(t):
@@ -265,39 +312,101 @@ def fcol(t):
     return t.permute(*reversed(range(t.dim())))
 
 
+def f_to_torch(a, pin=False, device=None):
+    """A Fortran-ordered numpy array as an F-contiguous torch view (pinned host or device)."""
+    import torch
+    t = torch.from_numpy(np.ascontiguousarray(np.asarray(a).transpose(tuple(reversed(range(a.ndim))))))
+    if pin:
+        t = t.pin_memory()
+    if device is not None:
+        t = t.to(device)
+    return fcol(t)
+
+
+def cols_of(a, k):
+    """The first k perturbation columns of [nmo, nocc, 3, natm] (or [nmo, nocc, ncol]) as [nmo, nocc, k]."""
+    return np.asfortranarray(a.reshape(a.shape[0], a.shape[1], -1, order="F")[:, :, :k])
+
+
+def with_cols(full, part, k):
+    """A copy of `full` [n1, n2, 3, natm] whose first k perturbation columns are `part`'s."""
+    out = np.array(full, order="F", copy=True)
+    flat = out.reshape(out.shape[0], out.shape[1], -1, order="F")
+    assert np.shares_memory(flat, out)
+    flat[:, :, :k] = np.asarray(part).reshape(out.shape[0], out.shape[1], k, order="F")
+    return out
+
+
+def setup_ctx(cphf_gb300, s, precision, local, cderi=None, **cfg):
+    ctx = cphf_gb300.Context(precision=precision, device=local, **cfg)
+    prepare_ctx(ctx, s, cderi)
+    return ctx
+
+
+def prepare_ctx(ctx, s, cderi=None, mo=None):
+    """set_cderi (+ grid) and make_response_preparation from the given (host or pinned) arrays."""
+    ctx.set_cderi(s.cderi if cderi is None else cderi, s.scale_j, s.scale_k, nao=s.nao)
+    if s.grid is not None:
+        ctx.set_grid(s.grid.ao, s.grid.weights, s.grid.fxc, s.nspin, s.grid.atom_offsets)
+    C, occ, e = mo if mo is not None else (s.mo_coeff, s.mo_occ, s.mo_energy)
+    if s.nspin == 1:
+        ctx.make_response_preparation(C[0], occ[0], e[0])
+    else:
+        ctx.make_response_preparation(C, occ, e)
+
+
+def run_apply_only(args, local):
+    """Time single operator applications (for launch lists and profiler captures)."""
+    import cphf_gb300
+    from cphf_gb300 import synth
+    cphf_gb300.build()
+    s = synth.make_system(args.workload, seed=args.seed)
+    nb = args.nb or 3 * s.natm
+    ctx = setup_ctx(cphf_gb300, s, args.precision, local)
+    rng = np.random.default_rng(args.seed + 1)
+    mo1 = [rng.standard_normal((s.nao, s.nocc[t], nb)) for t in range(s.nspin)]
+    mo1 = mo1 if s.nspin == 2 else mo1[0]
+    op = ctx.response_dimless_cphf_lowp if args.precision == "mixed" else ctx.response_dimless_cphf
+    for r in range(args.reps):
+        t0 = time.perf_counter()
+        op(mo1)
+        print(f"application {r}: {time.perf_counter() - t0:.4f} s ({args.workload}, nb={nb}, {args.precision})",
+              flush=True)
+
+
 def run_gpu(args, world, rank, local):
     import torch
     import cphf_gb300
     from cphf_gb300 import synth
 
+    t_run0 = time.perf_counter()
     torch.cuda.set_device(local)
     cphf_gb300.build()
+    t = time.perf_counter()
     s = synth.make_system(args.workload, seed=args.seed)
+    synth_s = time.perf_counter() - t
     nspin = s.nspin
+    nrhs = 3 * s.natm
     rhs_h = s.rhs if nspin == 2 else [s.rhs[0]]
-
-    def make_ctx(precision, **cfg):
-        ctx = cphf_gb300.Context(precision=precision, device=local, **cfg)
-        ctx.set_cderi(s.cderi, s.scale_j, s.scale_k)
-        if s.grid is not None:
-            ctx.set_grid(s.grid.ao, s.grid.weights, s.grid.fxc, nspin, s.grid.atom_offsets)
-        if nspin == 1:
-            ctx.make_response_preparation(s.mo_coeff[0], s.mo_occ[0], s.mo_energy[0])
-        else:
-            ctx.make_response_preparation(s.mo_coeff, s.mo_occ, s.mo_energy)
-        return ctx
+    arg = (lambda v: v if nspin == 2 else v[0])
+    dev = torch.device("cuda", local)
 
     weights = ROOT / "rstsr-showcase-hessian_gb300" / "cphf_gb300" / "mlp_weights.npy"
-    learned = weights.exists() and not args.no_learned and nspin == 1
+    learned = weights.exists() and not args.no_learned
     inner = {} if args.inner_tol is None else dict(inner_tol=args.inner_tol)
-    mixed = make_ctx("mixed", verify_residual=0, use_learned_guess=1 if learned else 0,
+    mixed_cfg = dict(verify_residual=args.verify, use_learned_guess=args.learned_mode if learned else 0,
                      residual_dfloat=args.residual, cuda_graphs=0 if args.no_graphs else 1, **inner)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    mixed = setup_ctx(cphf_gb300, s, "mixed", local, **mixed_cfg)
     if learned:
         mixed.set_mlp_weights(np.load(weights))
+    mixed.synchronize()
+    setup_resident_s = time.perf_counter() - t
+
     # device-resident inputs and outputs (F-contiguous views of C-ordered tensors)
-    rhs_d = [fcol(torch.from_numpy(np.ascontiguousarray(r.transpose(3, 2, 1, 0))).cuda()) for r in rhs_h]
-    out_d = [fcol(torch.empty(tuple(reversed(r.shape)), dtype=torch.float64, device="cuda")) for r in rhs_h]
-    arg = (lambda v: v if nspin == 2 else v[0])
+    rhs_d = [f_to_torch(r, device=dev) for r in rhs_h]
+    out_d = [fcol(torch.empty(tuple(reversed(r.shape)), dtype=torch.float64, device=dev)) for r in rhs_h]
     stream = torch.cuda.ExternalStream(mixed.stream)
 
     for _ in range(args.warmup):
@@ -321,6 +430,7 @@ def run_gpu(args, world, rank, local):
     clk = clocks.stop()
     t_step = ev0.elapsed_time(ev1) * 1e-3 / args.steps
     t_step = max_over_ranks(world, t_step)
+    x_mixed = [np.asfortranarray(o.cpu().numpy()) for o in out_d]
 
     # per-kernel-class breakdown: one more solve with the CUDA-event profiler on (which runs the
     # operator eagerly instead of replaying its graphs), outside the timed region
@@ -334,67 +444,154 @@ def run_gpu(args, world, rank, local):
     prof = mixed.profile_report()
     mixed.profile(False)
 
-    # end to end through the C ABI with pinned host buffers (copies inside the timed region)
-    rhs_p = [torch.from_numpy(np.ascontiguousarray(r.transpose(3, 2, 1, 0))).pin_memory() for r in rhs_h]
-    out_p = [torch.empty(tuple(reversed(r.shape)), dtype=torch.float64).pin_memory() for r in rhs_h]
-    rhs_pf = [fcol(t) for t in rhs_p]
-    out_pf = [fcol(t) for t in out_p]
-    h2d = sum(r.nbytes for r in rhs_h)
-    d2h = h2d
-    t = time.perf_counter()
-    for _ in range(args.steps):
-        mixed.solve_dimless_cphf(arg(rhs_pf), out=arg(out_pf))
-    t_e2e = max_over_ranks(world, (time.perf_counter() - t) / args.steps)
-    x_mixed = [o.numpy().transpose(3, 2, 1, 0).copy(order="F") for o in out_p]
-    tc_active = mixed.tensor_cores_active
-    mixed.close()  # release its device memory before the FP64 context is built
+    # what the trained network gains: the same solve without it (same context, same box)
+    gain = None
+    if learned and not args.no_learned_gain:
+        mixed.set_config(use_learned_guess=0)
+        eg0, eg1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        eg0.record(stream)
+        mixed.solve_dimless_cphf(arg(rhs_d), out=arg(out_d))
+        eg1.record(stream)
+        torch.cuda.synchronize()
+        st0 = mixed.last_stats
+        t_nolearn = eg0.elapsed_time(eg1) * 1e-3
+        gain = dict(with_s=t_step, without_s=t_nolearn, gain=(t_nolearn - t_step) / t_nolearn,
+                    mode=args.learned_mode,
+                    lowp_columns_with=stats[-1]["lowp_matvec_columns"], lowp_columns_without=st0["lowp_matvec_columns"],
+                    cycles_with=stats[-1]["cycles"], cycles_without=st0["cycles"])
+        mixed.set_config(use_learned_guess=args.learned_mode)
+
+    # end to end through the public API with pinned host buffers: per step the packed cderi
+    # upload, the preparation (Z/O, B planes) and the solve (rhs in, U1 out)
+    cderi_p = f_to_torch(s.cderi, pin=True)
+    mo_p = ([f_to_torch(c, pin=True) for c in s.mo_coeff[:nspin]], [np.asarray(o) for o in s.mo_occ[:nspin]],
+            [np.asarray(e) for e in s.mo_energy[:nspin]])
+    rhs_p = [f_to_torch(r, pin=True) for r in rhs_h]
+    out_p = [fcol(torch.empty(tuple(reversed(r.shape)), dtype=torch.float64).pin_memory()) for r in rhs_h]
     del rhs_d, out_d
+    n_e2e = args.steps if args.e2e_steps <= 0 else min(args.e2e_steps, args.steps)
+    h2d = (s.cderi.nbytes + sum(c.nbytes for c in s.mo_coeff[:nspin]) + sum(r.nbytes for r in rhs_h)
+           + (s.grid.ao.nbytes + s.grid.weights.nbytes + s.grid.fxc.nbytes if s.grid is not None else 0))
+    d2h = sum(r.nbytes for r in rhs_h)
+    e2e_times, setup_times = [], []
+    for _ in range(n_e2e):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        prepare_ctx(mixed, s, cderi=cderi_p, mo=mo_p)
+        mixed.synchronize()
+        setup_times.append(time.perf_counter() - t)
+        mixed.solve_dimless_cphf(arg(rhs_p), out=arg(out_p))
+        e2e_times.append(time.perf_counter() - t)
+    t_e2e = max_over_ranks(world, statistics.median(e2e_times))
+    setup_s = statistics.median(setup_times)
+    x_e2e = [np.asfortranarray(o.numpy()) for o in out_p]
+    e2e_same = max(float(np.abs(a - b).max()) for a, b in zip(x_e2e, x_mixed))
+    tc_active = mixed.tensor_cores_active
+
+    # finalize_cphf of the mixed solution on the mixed context (its response on the FP64-accurate
+    # operator) and the Hessian, for the accuracy comparison below
+    f1 = s.f1mo if nspin == 2 else s.f1mo[0]
+    s1 = s.s1mo if nspin == 2 else s.s1mo[0]
+    t = time.perf_counter()
+    m1_mx, me_mx = mixed.finalize_cphf(f1, s1, arg(x_mixed))
+    de_mx = mixed.get_cphf_hess(f1, s1, m1_mx, me_mx)
+    finalize_s = time.perf_counter() - t
+    m1_mx = m1_mx if nspin == 2 else [m1_mx]
+    me_mx = me_mx if nspin == 2 else [me_mx]
+    mixed.close()  # release its device memory before the FP64 context is built
+    del cderi_p
     torch.cuda.empty_cache()
 
-    # plain FP64 solve of the same system (the reference's arithmetic), timed once
-    fp64 = make_ctx("fp64", cphf_tol=args.fp64_tol, cphf_lindep=args.fp64_lindep)
-    fp64_res = None
-    if not args.no_fp64:
-        t = time.perf_counter()
-        x64 = fp64.solve_dimless_cphf(arg(rhs_h))
-        t_fp64 = time.perf_counter() - t
-        st64 = fp64.last_stats
-        x64 = x64 if nspin == 2 else [x64]
+    # ---- plain FP64 GPU solve (the reference's arithmetic) and the accuracy of the mixed solve
+    fp64 = setup_ctx(cphf_gb300, s, "fp64", local, cphf_tol=args.fp64_tol, cphf_lindep=args.fp64_lindep)
+    fp64_line, accuracy = None, {}
 
-    # verification outside the timed regions: FP64 residuals (on the first --verify-cols
-    # perturbations, all by default) and Hessian blocks
-    ncols_v = args.verify_cols if args.verify_cols > 0 else None
-    t_verify = [0.0]
-
-    def residual(x):
-        bs = [b.reshape(b.shape[0], b.shape[1], -1, order="F")[:, :, :ncols_v] for b in rhs_h]
-        xs = [xx.reshape(xx.shape[0], xx.shape[1], -1, order="F")[:, :, :ncols_v] for xx in x]
-        t = time.perf_counter()
-        y = fp64.response_dimless_cphf(arg([np.asfortranarray(v) for v in xs]))
-        t_verify[0] = time.perf_counter() - t
+    def residual_cols(x, k):
+        """native FP64 max_j ||b_j - (I+A)x_j||_2 over the first k columns, and the application time"""
+        bs = [cols_of(b, k) for b in rhs_h]
+        xs = [cols_of(v, k) for v in x]
+        fp64.synchronize()
+        t0 = time.perf_counter()
+        y = fp64.response_dimless_cphf(arg(xs))
+        t_app = time.perf_counter() - t0
         y = y if nspin == 2 else [y]
-        return max(float(np.linalg.norm((b - xx - yy).reshape(-1, b.shape[2], order="F"), axis=0).max())
-                   for b, xx, yy in zip(bs, xs, y))
+        r = max(float(np.linalg.norm((b - v - w).reshape(-1, k, order="F"), axis=0).max())
+                for b, v, w in zip(bs, xs, y))
+        return r, t_app
 
-    res_mixed = residual(x_mixed)
-    t_verify_mixed = t_verify[0]
-    hess_diff = None
     if not args.no_fp64:
-        fp64_res = residual(x64)
-        f1 = s.f1mo if nspin == 2 else s.f1mo[0]
-        s1 = s.s1mo if nspin == 2 else s.s1mo[0]
-        h = []
-        for x in (x_mixed, x64):
-            m1, me = fp64.finalize_cphf(f1, s1, arg(x))
-            h.append(fp64.get_cphf_hess(f1, s1, m1, me))
-        hess_diff = float(np.abs(h[0] - h[1]).max())
+        full = args.fp64_full or nrhs <= FULL_FP64_MAX_NRHS
+        if full:
+            t = time.perf_counter()
+            x64 = fp64.solve_dimless_cphf(arg(rhs_h))
+            t_fp64 = time.perf_counter() - t
+            st64 = fp64.last_stats
+            x64 = x64 if nspin == 2 else [x64]
+            res_mixed, t_app = residual_cols(x_mixed, nrhs)
+            res_64, _ = residual_cols(x64, nrhs)
+            m1_64, me_64 = fp64.finalize_cphf(f1, s1, arg(x64))
+            de_64 = fp64.get_cphf_hess(f1, s1, m1_64, me_64)
+            m1_64 = m1_64 if nspin == 2 else [m1_64]
+            accuracy = dict(columns=nrhs, atoms="all",
+                            u1_max_abs_diff=max(float(np.abs(a - b).max()) for a, b in zip(m1_mx, m1_64)),
+                            hessian_max_abs_diff=float(np.abs(de_mx - de_64).max()),
+                            mixed_residual_fp64=res_mixed, fp64_residual_fp64=res_64)
+            fp64_line = dict(value=t_fp64, unit="s", measured=True, aop_calls=st64["aop_calls"],
+                             aop_columns=st64["aop_columns"], cycles=st64["cycles"], tol=args.fp64_tol,
+                             lindep=args.fp64_lindep, application_s=t_app, application_cols=nrhs)
+        else:
+            # FP64 solve of the first k perturbation columns (the columns are independent
+            # systems): call count, and U1 / Hessian reference for those columns
+            k = args.fp64_cols
+            k = max(3, (k // 3) * 3)  # whole atoms
+            t = time.perf_counter()
+            x64 = fp64.solve_dimless_cphf(arg([cols_of(r, k) for r in rhs_h]))
+            t_sub = time.perf_counter() - t
+            st64 = fp64.last_stats
+            x64 = x64 if nspin == 2 else [x64]
+            # FP64 applications at k and at a wider width: cost model t0 + t1 nb; the wider one is
+            # also the native FP64 residual of the mixed solution on those columns
+            res_mixed_k, t_k = residual_cols(x_mixed, k)
+            w = min(args.fp64_app_cols, nrhs)
+            res_mixed_w, t_w = residual_cols(x_mixed, w)
+            t1 = (t_w - t_k) / max(w - k, 1)
+            t0 = max(t_k - t1 * k, 0.0)
+            per_call_full = t0 + t1 * nrhs
+            res_64, _ = residual_cols(x64, k)
+            # finalize of the subset columns in FP64; Hessian blocks of the subset's atoms from the
+            # mixed finalize with those columns replaced (every block of atoms 0..k/3-1)
+            natm_k = k // 3
+            f1k = [cols_of(v, k).reshape(v.shape[0], v.shape[1], 3, natm_k, order="F") for v in
+                   (s.f1mo[:nspin])]
+            s1k = [cols_of(v, k).reshape(v.shape[0], v.shape[1], 3, natm_k, order="F") for v in
+                   (s.s1mo[:nspin])]
+            x64k = [v.reshape(v.shape[0], v.shape[1], 3, natm_k, order="F") for v in x64]
+            m1k, mek = fp64.finalize_cphf(arg(f1k), arg(s1k), arg(x64k))
+            m1k = m1k if nspin == 2 else [m1k]
+            mek = mek if nspin == 2 else [mek]
+            hyb_m1 = [with_cols(a, b, k) for a, b in zip(m1_mx, m1k)]
+            hyb_me = [with_cols(a, b, k) for a, b in zip(me_mx, mek)]
+            de_hyb = fp64.get_cphf_hess(f1, s1, arg(hyb_m1), arg(hyb_me))
+            accuracy = dict(columns=k, atoms=f"0..{natm_k - 1} (every Hessian block with one of them)",
+                            u1_max_abs_diff=max(float(np.abs(cols_of(a, k) - cols_of(b, k)).max())
+                                                for a, b in zip(m1_mx, m1k)),
+                            hessian_max_abs_diff=float(np.abs(de_mx - de_hyb).max()),
+                            mixed_residual_fp64=max(res_mixed_k, res_mixed_w), mixed_residual_columns=w,
+                            fp64_residual_fp64=res_64)
+            fp64_line = dict(value=st64["aop_calls"] * per_call_full, unit="s", measured=False, extrapolated=True,
+                             aop_calls=st64["aop_calls"], cycles=st64["cycles"], tol=args.fp64_tol,
+                             lindep=args.fp64_lindep, subset_solve_s=t_sub, subset_columns=k,
+                             application_s={str(k): t_k, str(w): t_w}, per_call_full_s=per_call_full,
+                             how=(f"calls of a measured FP64 solve of {k} of {nrhs} columns x per-call time "
+                                  f"t0 + t1*{nrhs} from measured FP64 applications at {k} and {w} columns"))
+    fp64.close()
 
-    # roofline of the dominant kernel class in the timed region
-    hbm, bf16, peak_src = load_peaks()
+    # ---- roofline of the dominant kernel class in the timed region
+    hbm, bf16, bf16_sus, peak_src = load_peaks()
     dom_name, dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
     tensor_notes = {
         "kterm_tcgen05_f16x3": "FP16 hi/lo, the tensor pipe executes 3 split products",
-        "tgen_tcgen05_f16x3": "FP16 hi/lo, the tensor pipe executes 3 split products (twice: max, then planes)",
+        "tgen_tcgen05_f16x3": "FP16 hi/lo, the tensor pipe executes 3 split products",
         "wgen_tcgen05_f16x3": "FP16 hi/lo, the tensor pipe executes 3 split products",
         "term2_tcgen05_f16x3": "FP16 hi/lo, the tensor pipe executes 3 split products",
         "kterm_tcgen05_bf16x6_exact": "exact BF16 slices, the tensor pipe executes 21 slice products",
@@ -411,9 +608,10 @@ def run_gpu(args, world, rank, local):
                     peak_source="in-run cuBLAS FP64 GEMM 8192^3 (FP64 has no entry in MEASURED_PEAKS.json)")
     else:
         note = tensor_notes.get(dom_name, "")
-        roof = dict(bound="tensor", achieved=dom["flops"] / dom["ms"] / 1e9, peak=bf16, unit="TFLOP/s",
-                    peak_source=f"{peak_src} bf16 dense (FP16 runs at the same rate); achieved counts algorithmic "
-                                f"FLOPs" + (f"; {note}" if note else ""))
+        roof = dict(bound="tensor", achieved=dom["flops"] / dom["ms"] / 1e9, peak=bf16_sus, unit="TFLOP/s",
+                    peak_source=(f"{peak_src} bf16 dense sustained (the kernel is timed inside a "
+                                 f"{t_step:.0f} s solve; FP16 runs at the same rate; burst {bf16}); achieved "
+                                 f"counts algorithmic FLOPs") + (f"; {note}" if note else ""))
     # DRAM bytes per launch: the ratio of ncu-measured DRAM bytes to the algorithmic bytes of
     # the same kernel on a small case (profiles/), times this run's algorithmic bytes per launch
     traffic_ratio = {"kterm_tcgen05_f16x3": 1.262 / 1.18,        # tc_term1_kernel, rhf_nao300
@@ -436,43 +634,55 @@ def run_gpu(args, world, rank, local):
                 launches=dom["launches"], avg_launch_ms=dom["ms"] / dom["launches"],
                 share_of_step=dom["ms"] * 1e-3 / t_prof)
 
-    cpu = cpu_oracle_estimate(s, args.cpu_sample) if rank == 0 and not args.no_cpu else None
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        ncols = cpu_sample_cols(s, args.cpu_sample)
+        calls = fp64_line["aop_calls"] if (fp64_line and not fp64_line.get("measured")) else None
+        cal = cpu_oracle_calibrate(s, ncols, calls=calls)
+        if calls is not None:
+            cal["calls_source"] = f"the GPU FP64 solve of {fp64_line['subset_columns']} columns (same algorithm)"
+        cpu = cpu_oracle_record(cal, cpu_oracle_value(cal, cal["t1"]))
+
     st = stats[-1]
     line = dict(
         metric=METRIC, value=t_step, unit="s", n_gpus=args.gpus, steps=args.steps, warmup=args.warmup,
         ms_per_step=t_step * 1e3, higher_is_better=False, scaling="weak", vs_baseline=None,
         dtype=("f16x3 tensor-core operator / f32 / f64 defect correction"
-               + {0: " (fp64 residual)", 1: " (double-float residual)",
-                  2: " (residual: bf16x6 exact-slice tensor-core K term and XC + double-float)"}[args.residual]),
+               + {0: " (fp64 residuals)", 1: " (double-float residuals)",
+                  2: " (residuals: bf16x6 exact-slice tensor-core K term and XC + double-float)"}[args.residual]),
         data=f"synthetic (seeded generator, {args.workload}, seed {args.seed})",
         config=dict(workload=args.workload, description=WORKLOAD_DESC.get(args.workload, args.workload),
-                    precision="mixed", learned_guess=learned, residual_mode=args.residual,
+                    precision="mixed", learned=(f"mode {args.learned_mode}" if learned else None),
+                    residual_mode=args.residual, final_check=args.verify,
                     inner_tol=args.inner_tol if args.inner_tol is not None else 1e-6,
                     cuda_graphs=not args.no_graphs,
                     parallelism="replicas" if world > 1 else "single GPU",
                     l2="inputs larger than L2 (dense cderi FP64 %.1f GB)" % (s.nao ** 2 * s.naux * 8 / 1e9)),
-        fp64_plain=None if args.no_fp64 else dict(value=t_fp64, unit="s", aop_calls=st64["aop_calls"],
-                                                  cycles=st64["cycles"], tol=args.fp64_tol,
-                                                  lindep=args.fp64_lindep),
-        speedup_vs_fp64_plain=None if args.no_fp64 else t_fp64 / t_step,
-        residual=dict(mixed_verified=res_mixed, fp64_plain_verified=fp64_res, target=1e-8,
-                      verified_columns=ncols_v or int(np.prod(rhs_h[0].shape[2:])),
-                      fp64_operator_s=t_verify_mixed),
-        hessian_max_abs_diff_vs_fp64=hess_diff,
-        solve_stats=dict(refine_steps=st["refine_steps"], fp64_matvec_columns=st["fp64_matvec_columns"],
+        fp64_plain=fp64_line,
+        speedup_vs_fp64_plain=None if fp64_line is None else fp64_line["value"] / t_step,
+        speedup_e2e_vs_fp64_plain=None if fp64_line is None else fp64_line["value"] / t_e2e,
+        accuracy=accuracy or None,
+        solve_stats=dict(residual_max=st["residual_max"], residual_mode=st["residual_mode"],
+                         refine_steps=st["refine_steps"], fp64_matvec_columns=st["fp64_matvec_columns"],
                          lowp_matvec_columns=st["lowp_matvec_columns"], cycles=st["cycles"],
                          tensor_cores=tc_active),
+        learned_gain=gain,
         kernel_classes=dict(
             note="one profiled solve (eager operator, CUDA events per class) outside the timed region",
             solve_s=t_prof,
             **{k: dict(launches=v["launches"], ms=round(v["ms"], 3),
                        tflops=round(v["flops"] / max(v["ms"], 1e-9) / 1e9, 2),
                        gbs=round(v["bytes"] / max(v["ms"], 1e-9) / 1e6, 1)) for k, v in prof.items()}),
-        e2e=dict(value=t_e2e, unit="s", h2d_bytes_per_step=h2d, d2h_bytes_per_step=d2h),
+        e2e=dict(value=t_e2e, unit="s", h2d_bytes_per_step=int(h2d), d2h_bytes_per_step=int(d2h), steps=n_e2e,
+                 setup_s=setup_s, solve_s=t_e2e - setup_s, same_answer_max_abs=e2e_same,
+                 includes="packed cderi upload + make_response_preparation (Z/O, FP16 and BF16 planes of B) + "
+                          "solve with rhs in and U1 out, pinned host buffers"),
+        setup=dict(synth_s=synth_s, resident_setup_s=setup_resident_s, finalize_hessian_s=finalize_s),
         gpu_launches=int(launches),
         roofline=roof,
         cpu_baseline=None if cpu is None else {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         clocks=clk,
+        wall_s=time.perf_counter() - t_run0,
     )
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -481,7 +691,9 @@ def run_gpu(args, world, rank, local):
 def main():
     args = parse()
     world, rank, local = dist_setup(args)
-    if args.impl == "reference":
+    if args.apply_only:
+        run_apply_only(args, local)
+    elif args.impl == "reference":
         run_reference(args, world, rank)
     else:
         run_gpu(args, world, rank, local)

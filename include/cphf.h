@@ -18,8 +18,8 @@
  *    non-convergence, src/util/krylov_block.rs:188-194) the call returns a
  *    status code; cphf_last_error() gives the message.
  *  - One context per host thread; calls on a context are serialized on the
- *    context's CUDA stream (the reference's &mut self plugins,
- *    src/hessian/trait_rhess.rs:637-664).
+ *    context's CUDA stream (the reference's &mut self plugin methods,
+ *    src/hessian/trait_rhess.rs:162, 189 and src/hessian/trait_uhess.rs:152, 171).
  */
 #ifndef CPHF_H
 #define CPHF_H
@@ -60,11 +60,20 @@ typedef struct cphf_config {
   double residual_tol;       /* mixed: stop when max column ||b-(I+A)x||_2 < residual_tol (default 1e-8) */
   double inner_tol;          /* mixed: Krylov tol of each inner solve, relative to the residual (default 1e-6) */
   int64_t max_refine;        /* mixed: maximum defect-correction steps (default 6) */
-  int32_t use_learned_guess; /* use the MLP initial guess / preconditioner if weights are set (default 0) */
+  int32_t use_learned_guess; /* learned per-pair MLP (weights set by cphf_mlp_set_weights), default 0 = off.
+                                MIXED: 1 = left preconditioner of the inner solves, 2 = preconditioner and
+                                initial guess of the first inner solve (the guess costs one more operator
+                                application for its residual).  FP64: any non-zero value = initial guess
+                                x0 only (the Krylov iteration and stopping test stay the reference's). */
   int32_t verbose;           /* print per-cycle diagnostics like krylov_block.rs:148-151 (default 0) */
   int64_t aux_chunk;         /* aux functions per K-term chunk (default 0 = automatic) */
   int32_t tensor_cores;      /* mixed: 1 = tcgen05 split-FP16 K term (default), 0 = FP32 CUDA cores */
-  int32_t verify_residual;   /* mixed: recompute the final residual with the FP64 operator (default 1) */
+  int32_t verify_residual;   /* mixed: how the residual of every correction after the first is obtained and
+                                convergence decided.  0 = updated with the split-precision operator,
+                                r -= (I + A_lowp) d (no FP64-accurate application);  1 = recomputed with
+                                the native FP64 operator;  2 = recomputed with the FP64-accurate operator
+                                selected by residual_dfloat (default).  With 1 or 2 the solve returns only
+                                after a recomputed max_j ||b_j - (I+A)x_j||_2 < residual_tol. */
   int32_t fp64_every_step;   /* mixed: FP64 residual after every correction, not only the first (default 0) */
   int64_t xc_chunk_points;   /* grid points per XC chunk (default 0 = 8 GiB of intermediates) */
   int32_t residual_dfloat;   /* mixed: arithmetic of the correction residuals.  0 = native FP64;
@@ -73,7 +82,7 @@ typedef struct cphf_config {
                                 tensor cores as exact BF16 slice products (6 x 6 bits, ~1e-10 relative
                                 to the operand row maxima; default; without tensor cores it behaves
                                 as 1).
-                                The final verification (verify_residual) is always native FP64. */
+                                verify_residual = 1 recomputes the later residuals in native FP64. */
   int32_t cuda_graphs;       /* mixed: replay each block width's split-precision operator application
                                 from a captured CUDA graph (default 1); bypassed while profiling */
 } cphf_config;
@@ -90,6 +99,9 @@ typedef struct cphf_stats {
   int64_t lowp_matvec_columns;  /* columns pushed through the split-precision operator */
   int64_t refine_steps;         /* defect-correction steps (mixed precision) */
   double seconds;               /* wall time of the call */
+  int64_t residual_mode;        /* how residual_max was computed: 0 native FP64, 1 double-float GEMMs,
+                                   2 double-float + exact BF16 slice products on the tensor cores,
+                                   3 updated with the split-precision operator, -1 not computed */
 } cphf_stats;
 
 typedef struct cphf_ctx cphf_ctx;
@@ -137,6 +149,36 @@ int32_t cphf_ctx_profile_report(cphf_ctx* ctx, cphf_prof_entry* out, int32_t max
 cphf_status cphf_rijk_set_cderi(cphf_ctx* ctx, const double* cderi, int64_t nao, int64_t naux,
                                 double scale_j, double scale_k);
 
+/* ---- cderi construction: two-centre metric decomposition and triangular solve (FP64) --- */
+/* Outcome of a j2c decomposition. */
+typedef struct cphf_j2c_info {
+  int32_t eig_fallback;      /* 1 when the eigenvalue-clamping fallback was taken */
+  int32_t jacobi_sweeps;     /* sweeps of the fallback's Jacobi eigensolver */
+  double min_diag;           /* min diag(U) of the returned factor */
+  double seconds_decompose;  /* wall time of the decomposition */
+  double seconds_solve;      /* wall time of the triangular solve (cphf_rijk_set_j3c) */
+} cphf_j2c_info;
+
+/* decomp_j2c_cd(j2c, threshold, Upper) (src/ri_jk/pure_decompose.rs:29-57): j2c [naux, naux]
+ * = U^T U, U upper triangular written to j2c_u [naux, naux] (zeros below the diagonal).  When
+ * the factorisation fails or min diag(U) <= threshold, the eigenvalues of j2c are clamped at
+ * the threshold and the rebuilt matrix is factored without a further check (pure_decompose.rs:
+ * 44-51).  threshold < 0 means no fallback: a failed factorisation returns CPHF_ERR_NONFINITE
+ * (the reference panics, pure_decompose.rs:56).  info may be NULL. */
+cphf_status cphf_j2c_decompose(cphf_ctx* ctx, const double* j2c, int64_t naux, double threshold, double* j2c_u,
+                               cphf_j2c_info* info);
+/* generate_cderi_with_decomp (src/ri_jk/hess_r.rs:1725-1735) with the options of
+ * RHessRIJK::new_without_cderi (hess_r.rs:1752: Cholesky, threshold 1e-14, Upper) from
+ * caller-supplied integrals, then RHessRIJK::new_with_cderi on the result:
+ *   j3c [nao*(nao+1)/2, naux] packed (mu nu|P) (same layout as cphf_rijk_set_cderi's cderi),
+ *   j2c [naux, naux] (P|Q);  cderi = j3c U^-1 with j2c = U^T U (solve_by_j2c(j3c, Right,
+ *   flip_uplo = false), pure_decompose.rs:205-252), FP64 on the GPU.
+ * The RI-JK plugin then uses this cderi exactly as if passed to cphf_rijk_set_cderi. */
+cphf_status cphf_rijk_set_j3c(cphf_ctx* ctx, const double* j3c, const double* j2c, int64_t nao, int64_t naux,
+                              double scale_j, double scale_k, double threshold, cphf_j2c_info* info);
+/* Copy the RI-JK plugin's packed cderi [nao*(nao+1)/2, naux] out (host or device pointer). */
+cphf_status cphf_rijk_get_cderi(cphf_ctx* ctx, double* cderi);
+
 /* ---- XC plugin (LDA / XCDenType::RHO, src/xceff/flags.rs:33-55) ----------------------- */
 /* RHessKSNIMatmul / UHessKSNIMatmul with intmd["cpks_fxc"] (src/numint_matmul/hess_rks.rs:814-824, 895):
  *   ao      [ngrids, nao]  AO values (derivative order 0), the reference's get_cached_ao(0) tensor
@@ -151,13 +193,14 @@ cphf_status cphf_xc_set_grid(cphf_ctx* ctx, const double* ao, const double* weig
 cphf_status cphf_set_nao(cphf_ctx* ctx, int64_t nao);
 
 /* ---- response preparation and response (RHessElecInteractAPI) --------------------------- */
-/* make_response_preparation (src/hessian/trait_rhess.rs:637, hess_r.rs:1911-1914,
+/* make_response_preparation (src/hessian/trait_rhess.rs:162, trait_uhess.rs:152; hess_r.rs:1911-1914,
  * hess_rks.rs:886-889) plus the orbital energies the CPHF driver keeps (rscf.rs:21-25):
  *   mo_coeff[s] [nao, nmo], mo_occ[s] [nmo], mo_energy[s] [nmo], s < nspin (1 = RHF/RKS, 2 = UHF/UKS). */
 cphf_status cphf_prepare(cphf_ctx* ctx, int32_t nspin, const double* const* mo_coeff,
                          const double* const* mo_occ, const double* const* mo_energy, int64_t nmo);
 
-/* get_response_bra summed over the set plugins (rscf.rs:210-220 loop body):
+/* get_response_bra (src/hessian/trait_rhess.rs:189, trait_uhess.rs:171) summed over the set
+ * plugins (rscf.rs:210-220 loop body):
  *   bra[s], out[s] [nao, nocc_s, nprop].
  *   RHF: hess_r.rs:1916-1953 (+ hess_rks.rs:891-908); UHF: hess_u.rs:270-313 (+ hess_uks.rs:740-764). */
 cphf_status cphf_response_bra(cphf_ctx* ctx, const double* const* bra, int64_t nprop,
@@ -183,7 +226,9 @@ cphf_status cphf_response_dimless_lowp(cphf_ctx* ctx, const double* const* mo1, 
 cphf_status cphf_solve_dimless_cphf(cphf_ctx* ctx, const double* const* rhs, int64_t nprop,
                                     const double* const* x0, double* const* mo1, cphf_stats* stats);
 /* finalize_cphf (rscf.rs:328-353, uscf.rs:365-406): f1mo[s], s1mo[s] [nmo, nocc_s, 3, natm];
- * mo1[s] in/out; mo_e1[s] [nocc_s, nocc_s, 3, natm] out. */
+ * mo1[s] in/out; mo_e1[s] [nocc_s, nocc_s, 3, natm] out.  Its one response_mo (rscf.rs:342)
+ * runs in native FP64 on an FP64 context and in the FP64-accurate arithmetic selected by
+ * residual_dfloat on a MIXED context. */
 cphf_status cphf_finalize_cphf(cphf_ctx* ctx, const double* const* f1mo, const double* const* s1mo,
                                int64_t natm, double* const* mo1, double* const* mo_e1);
 /* get_cphf_hess (rscf.rs:371-399, uscf.rs:408-446): de [3, 3, natm, natm]. */

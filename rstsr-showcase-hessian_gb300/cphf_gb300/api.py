@@ -1,7 +1,7 @@
 """ctypes binding of libcphf (include/cphf.h) with the reference's call surface.
 
 Method names follow the reference crate: ``make_response_preparation`` and
-``get_response_bra`` of ``RHessElecInteractAPI`` (``src/hessian/trait_rhess.rs:637,664``),
+``get_response_bra`` of ``RHessElecInteractAPI`` (``src/hessian/trait_rhess.rs:162,189``; UHF ``trait_uhess.rs:152,171``),
 ``response_mo`` / ``response_dimless_cphf`` / ``solve_dimless_cphf`` /
 ``finalize_cphf`` / ``get_cphf_hess`` of ``RHessSCF`` / ``UHessSCF``
 (``src/hessian/rscf.rs``, ``uscf.rs``) and ``krylov_block``
@@ -37,7 +37,7 @@ EXPORTS = [
     "cphf_dense_op_destroy", "cphf_copy", "cphf_mlp_set_weights", "cphf_ctx_tensor_cores_active",
     "cphf_ctx_profile", "cphf_ctx_profile_report", "cphf_mlp_get_weights", "cphf_mlp_features",
     "cphf_mlp_forward", "cphf_mlp_loss_grad", "cphf_mlp_train", "cphf_rij_noalloc_capacity",
-    "cphf_rij_response_bra_noalloc",
+    "cphf_rij_response_bra_noalloc", "cphf_j2c_decompose", "cphf_rijk_set_j3c", "cphf_rijk_get_cderi",
 ]
 MLP_NWEIGHTS = 4546
 
@@ -89,6 +89,20 @@ class Stats(ctypes.Structure):
         ("lowp_matvec_columns", ctypes.c_int64),
         ("refine_steps", ctypes.c_int64),
         ("seconds", ctypes.c_double),
+        ("residual_mode", ctypes.c_int64),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class J2cInfo(ctypes.Structure):
+    _fields_ = [
+        ("eig_fallback", ctypes.c_int32),
+        ("jacobi_sweeps", ctypes.c_int32),
+        ("min_diag", ctypes.c_double),
+        ("seconds_decompose", ctypes.c_double),
+        ("seconds_solve", ctypes.c_double),
     ]
 
     def as_dict(self):
@@ -156,6 +170,9 @@ def load_library():
         "cphf_mlp_forward": ([vp, vp, i64, vp, i32], i32),
         "cphf_mlp_loss_grad": ([vp, vp, vp, i64, ctypes.POINTER(ctypes.c_float), vp], i32),
         "cphf_mlp_train": ([vp, vp, vp, i64, i64, i64, ctypes.c_float, ctypes.c_uint64, vp], i32),
+        "cphf_j2c_decompose": ([vp, vp, i64, dbl, vp, ctypes.POINTER(J2cInfo)], i32),
+        "cphf_rijk_set_j3c": ([vp, vp, vp, i64, i64, dbl, dbl, dbl, ctypes.POINTER(J2cInfo)], i32),
+        "cphf_rijk_get_cderi": ([vp, vp], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -313,6 +330,44 @@ class Context:
         k = _Keep()
         self._check(self.lib.cphf_rijk_set_cderi(self.h, k.ptr(cderi), nao, naux, scale_j, scale_k))
         self.nao = nao
+        self.naux = naux
+
+    def j2c_decompose(self, j2c, threshold=1e-14):
+        """``decomp_j2c_cd(j2c, threshold, Upper)`` (src/ri_jk/pure_decompose.rs:29-57) on the GPU:
+        returns ``(U, info)`` with ``j2c = U^T U``; ``threshold=None`` disables the fallback."""
+        naux = j2c.shape[0]
+        U = np.zeros((naux, naux), order="F")
+        info = J2cInfo()
+        k = _Keep()
+        self._check(self.lib.cphf_j2c_decompose(self.h, k.ptr(j2c), naux, -1.0 if threshold is None else threshold,
+                                                k.ptr(U), ctypes.byref(info)))
+        return U, info.as_dict()
+
+    def set_j3c(self, j3c, j2c, scale_j=1.0, scale_k=1.0, threshold=1e-14, nao=None):
+        """``generate_cderi_with_decomp`` + ``new_with_cderi`` (src/ri_jk/hess_r.rs:1725-1735,
+        1752): cderi = j3c U^-1 with j2c = U^T U, built on the GPU in FP64; returns the info dict."""
+        nao_tp, naux = j3c.shape
+        if nao is None:
+            nao = int(round((np.sqrt(8 * nao_tp + 1) - 1) / 2))
+        if nao * (nao + 1) // 2 != nao_tp:
+            raise CphfError(ERR_SHAPE, "j3c rows are not a packed triangle")
+        info = J2cInfo()
+        k = _Keep()
+        self._check(self.lib.cphf_rijk_set_j3c(self.h, k.ptr(j3c), k.ptr(j2c), nao, naux, scale_j, scale_k,
+                                               -1.0 if threshold is None else threshold, ctypes.byref(info)))
+        self.nao = nao
+        self.naux = naux
+        return info.as_dict()
+
+    def get_cderi(self, out=None):
+        """The RI-JK plugin's packed cderi ``[nao_tp, naux]`` (host array, or into ``out``)."""
+        if out is None:
+            if getattr(self, "naux", None) is None:
+                raise CphfError(ERR_STATE, "RI-JK plugin not set")
+            out = np.zeros((self.nao * (self.nao + 1) // 2, self.naux), order="F")
+        k = _Keep()
+        self._check(self.lib.cphf_rijk_get_cderi(self.h, k.ptr(out)))
+        return out
 
     def set_nao(self, nao):
         self._check(self.lib.cphf_set_nao(self.h, nao))

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "ctx.cuh"
+#include "decompose.cuh"
 #include "kernels.cuh"
 #include "mlp.cuh"
 
@@ -108,13 +109,12 @@ void unpack_krylov(cphf_ctx* c, const double* src, int64_t nprop, double* const*
 }
 
 void check_finite(cphf_ctx* c, const double* dev, int64_t n, const char* what) {
-  c->k_info.ensure(sizeof(int), c->counter());
-  DevBuf tmp;
-  tmp.ensure(sizeof(int), c->counter());
-  CPHF_CUDA(cudaMemsetAsync(tmp.p, 0, sizeof(int), c->stream));
-  launch_count_nonfinite(dev, n, tmp.as<int>(), c->stream);
+  // context-owned counter: no allocation per call
+  c->k_finite.ensure(sizeof(int), c->counter());
+  CPHF_CUDA(cudaMemsetAsync(c->k_finite.p, 0, sizeof(int), c->stream));
+  launch_count_nonfinite(dev, n, c->k_finite.as<int>(), c->stream);
   int bad = 0;
-  CPHF_CUDA(cudaMemcpyAsync(&bad, tmp.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CPHF_CUDA(cudaMemcpyAsync(&bad, c->k_finite.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CPHF_CUDA(cudaStreamSynchronize(c->stream));
   if (bad) throw Error(CPHF_ERR_NONFINITE, std::string("non-finite values in ") + what);
 }
@@ -146,7 +146,7 @@ cphf_status cphf_config_default(cphf_config* cfg) {
   cfg->verbose = 0;
   cfg->aux_chunk = 0;
   cfg->tensor_cores = 1;
-  cfg->verify_residual = 1;
+  cfg->verify_residual = 2;
   cfg->fp64_every_step = 0;
   cfg->xc_chunk_points = 0;
   cfg->residual_dfloat = 2;
@@ -269,24 +269,97 @@ cphf_status cphf_set_nao(cphf_ctx* c, int64_t nao) {
   });
 }
 
+// The packed cderi in c->cderi_tp becomes the RI-JK plugin's B (dense copy, state reset).
+static void install_cderi(cphf_ctx* c, int64_t nao, int64_t naux, double scale_j, double scale_k) {
+  const int64_t nao_tp = nao * (nao + 1) / 2;
+  c->nao = nao;
+  c->naux = naux;
+  c->scale_j = scale_j;
+  c->scale_k = scale_k;
+  check_finite(c, c->cderi_tp.as<double>(), nao_tp * naux, "cderi");
+  c->Bd.ensure((size_t)nao * nao * naux * 8, c->counter());
+  launch_unpack_cderi(c->cderi_tp.as<double>(), nao, naux, c->Bd.as<double>(), c->stream);
+  c->has_rijk = true;
+  c->prepared = false;
+  lowp_release(c);
+  CPHF_CUDA(cudaStreamSynchronize(c->stream));
+}
+
 cphf_status cphf_rijk_set_cderi(cphf_ctx* c, const double* cderi, int64_t nao, int64_t naux,
                                 double scale_j, double scale_k) {
   return guarded(c, [&] {
     CPHF_CHECK_ARG(nao > 0 && naux > 0, "nao and naux must be positive");
     CPHF_CHECK_SHAPE(!c->has_xc || c->nao == nao, "nao differs from the XC grid's");
     const int64_t nao_tp = nao * (nao + 1) / 2;
-    c->nao = nao;
-    c->naux = naux;
-    c->scale_j = scale_j;
-    c->scale_k = scale_k;
     c->cderi_tp.ensure((size_t)nao_tp * naux * 8, c->counter());
     copy_in(c, c->cderi_tp.p, cderi, (size_t)nao_tp * naux * 8);
-    check_finite(c, c->cderi_tp.as<double>(), nao_tp * naux, "cderi");
-    c->Bd.ensure((size_t)nao * nao * naux * 8, c->counter());
-    launch_unpack_cderi(c->cderi_tp.as<double>(), nao, naux, c->Bd.as<double>(), c->stream);
-    c->has_rijk = true;
-    c->prepared = false;
-    lowp_release(c);
+    install_cderi(c, nao, naux, scale_j, scale_k);
+  });
+}
+
+static void fill_j2c_info(cphf_j2c_info* info, const J2cDecomp& d, double t_dec, double t_solve) {
+  if (!info) return;
+  info->eig_fallback = d.fallback ? 1 : 0;
+  info->jacobi_sweeps = d.sweeps;
+  info->min_diag = d.min_diag;
+  info->seconds_decompose = t_dec;
+  info->seconds_solve = t_solve;
+}
+
+cphf_status cphf_j2c_decompose(cphf_ctx* c, const double* j2c, int64_t naux, double threshold, double* j2c_u,
+                               cphf_j2c_info* info) {
+  return guarded(c, [&] {
+    CPHF_CHECK_ARG(naux > 0, "naux must be positive");
+    CPHF_CHECK_ARG(j2c_u != nullptr, "null output");
+    DecompWork w;
+    DevBuf m;
+    m.ensure((size_t)naux * naux * 8, c->counter());
+    copy_in(c, m.p, j2c, (size_t)naux * naux * 8);
+    check_finite(c, m.as<double>(), naux * naux, "j2c");
+    const auto t0 = std::chrono::steady_clock::now();
+    const J2cDecomp d = j2c_cholesky(c, m.as<double>(), naux, threshold, w);
+    const double t_dec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    copy_out(c, j2c_u, w.U.p, (size_t)naux * naux * 8);
+    CPHF_CUDA(cudaStreamSynchronize(c->stream));
+    fill_j2c_info(info, d, t_dec, 0.0);
+  });
+}
+
+cphf_status cphf_rijk_set_j3c(cphf_ctx* c, const double* j3c, const double* j2c, int64_t nao, int64_t naux,
+                              double scale_j, double scale_k, double threshold, cphf_j2c_info* info) {
+  return guarded(c, [&] {
+    CPHF_CHECK_ARG(nao > 0 && naux > 0, "nao and naux must be positive");
+    CPHF_CHECK_SHAPE(!c->has_xc || c->nao == nao, "nao differs from the XC grid's");
+    const int64_t nao_tp = nao * (nao + 1) / 2;
+    c->cderi_tp.ensure((size_t)nao_tp * naux * 8, c->counter());
+    copy_in(c, c->cderi_tp.p, j3c, (size_t)nao_tp * naux * 8);
+    check_finite(c, c->cderi_tp.as<double>(), nao_tp * naux, "j3c");
+    J2cDecomp d;
+    double t_dec = 0.0, t_solve = 0.0;
+    {
+      DecompWork w;
+      DevBuf m;
+      m.ensure((size_t)naux * naux * 8, c->counter());
+      copy_in(c, m.p, j2c, (size_t)naux * naux * 8);
+      check_finite(c, m.as<double>(), naux * naux, "j2c");
+      const auto t0 = std::chrono::steady_clock::now();
+      d = j2c_cholesky(c, m.as<double>(), naux, threshold, w);
+      const auto t1 = std::chrono::steady_clock::now();
+      solve_by_j2c_right(c, c->cderi_tp.as<double>(), nao_tp, naux, w);
+      CPHF_CUDA(cudaStreamSynchronize(c->stream));
+      const auto t2 = std::chrono::steady_clock::now();
+      t_dec = std::chrono::duration<double>(t1 - t0).count();
+      t_solve = std::chrono::duration<double>(t2 - t1).count();
+    }
+    install_cderi(c, nao, naux, scale_j, scale_k);
+    fill_j2c_info(info, d, t_dec, t_solve);
+  });
+}
+
+cphf_status cphf_rijk_get_cderi(cphf_ctx* c, double* cderi) {
+  return guarded(c, [&] {
+    CPHF_CHECK_ARG(c->has_rijk, "RI-JK plugin not set");
+    copy_out(c, cderi, c->cderi_tp.p, (size_t)c->nao * (c->nao + 1) / 2 * c->naux * 8);
     CPHF_CUDA(cudaStreamSynchronize(c->stream));
   });
 }
@@ -380,6 +453,7 @@ cphf_status cphf_prepare(cphf_ctx* c, int32_t nspin, const double* const* mo_coe
       SpinState& sp = c->spin[s];
       sp.nmo = nmo;
       sp.nocc = nocc;
+      sp.iaia.release();  // learned-guess features of the previous orbitals
       sp.C.ensure((size_t)nao * nmo * 8, c->counter());
       copy_in(c, sp.C.p, mo_coeff[s], (size_t)nao * nmo * 8);
       sp.e.ensure((size_t)nmo * 8, c->counter());
@@ -479,37 +553,37 @@ cphf_status cphf_solve_dimless_cphf(cphf_ctx* c, const double* const* rhs, int64
     check_finite(c, b, n * nprop, "rhs");
     if (x0) pack_krylov(c, x0, nprop, xg);
     const double* x0p = x0 ? xg : nullptr;
-    // learned initial guess and left preconditioner (convergence is still decided on the unpreconditioned FP64 residual)
-    DevBuf pre;
+    // Learned initial guess / left preconditioner, in context-owned buffers (no allocation per
+    // solve).  Mixed precision: the preconditioner m acts on the inner solves only, whose
+    // convergence the outer FP64-accurate residual judges; mode 2 also starts the first inner
+    // solve from the guess (one more operator application for its residual).  FP64: the guess
+    // is only the initial x0, so the Krylov iteration and its stopping test are the
+    // reference's unmodified ones (krylov_block.rs:86-87, 130-157).
     double* m = nullptr;
+    const bool mixed = c->cfg.precision == CPHF_PRECISION_MIXED;
     if (c->cfg.use_learned_guess) {
       mlp_require(c);
       if (c->spin[0].iaia.p == nullptr) mlp_prepare_iaia(c);
-      pre.ensure((size_t)n * 8 * (1 + nprop), c->counter());
-      m = pre.as<double>();
-      double* guess = m + n;
-      mlp_guess(c, b, nprop, guess, m);
-      if (!x0p) x0p = guess;
+      c->k_pre.ensure((size_t)n * 8 * (1 + nprop), c->counter());
+      double* mbuf = c->k_pre.as<double>();
+      double* guess = mbuf + n;
+      const bool want_guess = !mixed || c->cfg.use_learned_guess == 2;
+      mlp_guess(c, b, nprop, guess, mixed ? mbuf : nullptr);
+      if (mixed) m = mbuf;
+      if (!x0p && want_guess) x0p = guess;
     }
-    if (c->cfg.precision == CPHF_PRECISION_MIXED) {
+    if (mixed) {
       converged = solve_mixed(c, b, x0p, nprop, x, &st, m);
     } else {
       KrylovParams p{c->cfg.cphf_tol, c->cfg.cphf_lindep, c->cfg.cphf_max_cycle, c->cfg.cphf_max_space,
                      c->cfg.verbose != 0};
       DeviceOp op = [&](const double* xin, int64_t nb, double* yout) {
         response_mo_fp64(c, xin, nb, yout, true);
-        if (m) launch_apply_precond(m, xin, yout, n, nb, c->stream);
         st.fp64_matvec_columns += nb;
       };
-      const double* bp = b;
-      DevBuf bm;
-      if (m) {
-        bm.ensure((size_t)n * nprop * 8, c->counter());
-        launch_scale_rows_by(m, b, bm.as<double>(), n, nprop, c->stream);
-        bp = bm.as<double>();
-      }
-      converged = krylov_device(c, op, bp, x0p, n, nprop, p, x, &st);
+      converged = krylov_device(c, op, b, x0p, n, nprop, p, x, &st);
       st.residual_max = -1.0;  // not evaluated by the plain solver (the reference does not either)
+      st.residual_mode = -1;
     }
     unpack_krylov(c, x, nprop, mo1);
     CPHF_CUDA(cudaStreamSynchronize(c->stream));
@@ -542,7 +616,14 @@ cphf_status cphf_finalize_cphf(cphf_ctx* c, const double* const* f1mo, const dou
     pack_krylov(c, mo1, nprop, x);
     pack_krylov(c, f1mo, nprop, f1);
     pack_krylov(c, s1mo, nprop, s1);
-    response_mo_fp64(c, x, nprop, resp, false);  // rscf.rs:342
+    {
+      // rscf.rs:342.  A mixed-precision context evaluates this response with its FP64-accurate
+      // operator (residual_dfloat: exact-slice tensor cores + double-float by default), a
+      // plain FP64 context with native FP64.
+      const bool mixed = c->cfg.precision == CPHF_PRECISION_MIXED && c->lowp;
+      AccurateScope scope(c, mixed ? c->cfg.residual_dfloat : 0);
+      response_mo_fp64(c, x, nprop, resp, false);
+    }
     int64_t off = 0, offe = 0;
     for (int s = 0; s < c->nspin; ++s) {
       const SpinState& sp = c->spin[s];

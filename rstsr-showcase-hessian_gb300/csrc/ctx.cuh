@@ -214,7 +214,7 @@ struct cphf_ctx {
   // scratch (grown on demand)
   cphf::DevBuf ws_gemm, s_c1, s_resp, s_T, s_W, s_d, s_ket, s_rho, s_y, s_x, s_misc, s_host_io;
   cphf::DevBuf k_xs, k_ax, k_h, k_g, k_b, k_xacc, k_x1, k_axt, k_coef, k_ip, k_keep, k_part, k_idx,
-      k_hw, k_info, k_r, k_norm;
+      k_hw, k_info, k_r, k_norm, k_finite, k_pre;
 
   std::unique_ptr<cphf::LowpState> lowp;
   std::unique_ptr<cphf::MlpState> mlp;
@@ -291,5 +291,18 @@ double fp64_residual(cphf_ctx* c, const double* b, const double* x, int64_t nset
 // mixed-precision support
 void lowp_prepare(cphf_ctx* c);
 void lowp_release(cphf_ctx* c);
+
+// Scope in which the FP64 operator (response_mo_fp64) runs in the FP64-accurate arithmetic of
+// the mixed context: mode 0 native FP64, 1 double-float GEMMs, 2 double-float plus the RI-K
+// term and XC contractions as exact BF16 slice products on the tensor cores.  `used` is the
+// mode in effect (2 falls back to 1 where no tensor-core contraction applies).
+struct AccurateScope {
+  cphf_ctx* c;
+  int used = 0;
+  AccurateScope(cphf_ctx* ctx, int mode);
+  ~AccurateScope();
+  AccurateScope(const AccurateScope&) = delete;
+  AccurateScope& operator=(const AccurateScope&) = delete;
+};
 
 }  // namespace cphf

@@ -6,7 +6,8 @@
 // accumulation in TMEM (tc_gemm.cu).  Its error (~1e-6 relative) is removed by defect
 // correction: each step solves (I + A_lowp) d = r with the device Krylov solver (FP64
 // basis, orthogonalisation and projected solve), then recomputes r = b - (I + A) x with
-// the FP64 operator, until max_j ||r_j||_2 < residual_tol.
+// an FP64-accurate operator (exact BF16 slice products on the tensor cores plus
+// double-float GEMMs by default, or native FP64), until max_j ||r_j||_2 < residual_tol.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -332,6 +333,21 @@ void lowp_apply(cphf_ctx* c, const double* x, int64_t nb, double* y) {
   L.graphs.push_back(g);
 }
 
+AccurateScope::AccurateScope(cphf_ctx* ctx, int mode) : c(ctx) {
+  const bool tc = c->lowp && c->lowp->use_tc && oz_available(c);
+  c->f64_emulate = mode != 0;
+  c->oz_kterm = mode == 2 && c->has_rijk && tc && oz_supported(c);
+  c->oz_xc = mode == 2 && c->has_xc && tc;
+  // mode 2 without any tensor-core contraction available is the double-float operator
+  used = mode == 2 && !(c->oz_kterm || c->oz_xc) ? 1 : mode;
+}
+
+AccurateScope::~AccurateScope() {
+  c->f64_emulate = false;
+  c->oz_kterm = false;
+  c->oz_xc = false;
+}
+
 bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, double* x, cphf_stats* st,
                  const double* m) {
   if (!c->lowp) lowp_prepare(c);
@@ -366,12 +382,22 @@ bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, d
     st->lowp_matvec_columns += nb;
   };
   // Defect correction.  Step 0 solves with the full right-hand side; its residual is the one
-  // that must be exact, so it is recomputed with the FP64 operator: r1 = b - (I + A) x1.
-  // Later corrections d are O(|r1|), so the update r -= (I + A_lowp) d carries an error of
-  // only eps_lowp |d| ~ eps_lowp^2 |b|, far below the tolerance; the final residual is
-  // optionally recomputed with the FP64 operator (verify_residual).
+  // that must be exact, so it is recomputed with the FP64-accurate operator (residual_dfloat):
+  // r1 = b - (I + A) x1.  With verify_residual on (1 native FP64, 2 the residual_dfloat
+  // operator) every later residual is recomputed the same way and convergence is decided only
+  // on a recomputed residual, so the solve measures its own final ||b - (I+A)x||.  With it off,
+  // later corrections d are O(|r1|) and the update r -= (I + A_lowp) d carries an error of
+  // only eps_lowp |d| ~ eps_lowp^2 |b|, far below the tolerance.
+  auto accurate_residual = [&](int mode) {
+    AccurateScope scope(c, mode);
+    res = fp64_residual(c, b, x, nset, r, st);
+    st->residual_mode = scope.used;
+  };
+  const int first_mode = c->cfg.residual_dfloat;
+  const int final_mode = c->cfg.verify_residual == 1 ? 0 : c->cfg.verify_residual == 2 ? first_mode : -1;
   const double update_margin = 0.5;
   bool done = res < c->cfg.residual_tol;
+  st->residual_mode = 0;  // |b| itself is exact
   for (int64_t step = 0; step < c->cfg.max_refine && !done; ++step) {
     // solve (I + A_lowp) d' = r / |r|  (relative tolerances), d = |r| d'
     const double scale = res > 0.0 ? res : 1.0;
@@ -394,23 +420,17 @@ bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, d
     launch_axpby(scale, dlt, 0.0, dlt, n * nset, s);
     launch_axpby(1.0, dlt, 1.0, x, n * nset, s);
     st->refine_steps += 1;
-    if (step == 0 || c->cfg.fp64_every_step) {
-      c->f64_emulate = c->cfg.residual_dfloat != 0;
-      c->oz_kterm = c->cfg.residual_dfloat == 2 && c->has_rijk && c->lowp->use_tc && oz_available(c) &&
-                    oz_supported(c);
-      c->oz_xc = c->cfg.residual_dfloat == 2 && c->has_xc && c->lowp->use_tc && oz_available(c);
-      try {
-        res = fp64_residual(c, b, x, nset, r, st);
-      } catch (...) {
-        c->f64_emulate = false;
-        c->oz_kterm = false;
-        c->oz_xc = false;
-        throw;
-      }
-      c->f64_emulate = false;
-      c->oz_kterm = false;
-      c->oz_xc = false;
+    const char* how;
+    if (step == 0 || c->cfg.fp64_every_step || final_mode >= 0) {
+      const int mode = (step == 0 || final_mode < 0) ? first_mode : final_mode;
+      accurate_residual(mode);
       done = res < c->cfg.residual_tol;
+      if (done && final_mode >= 0 && mode != final_mode) {
+        // converged on the first correction's operator: confirm with the final-check operator
+        accurate_residual(final_mode);
+        done = res < c->cfg.residual_tol;
+      }
+      how = "recomputed";
     } else {
       lowp_apply(c, dlt, nset, adl);
       st->lowp_matvec_columns += nset;
@@ -420,16 +440,13 @@ bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, d
       res = 0.0;
       for (double v : h) res = std::max(res, std::sqrt(v));
       if (!std::isfinite(res)) throw Error(CPHF_ERR_NONFINITE, "non-finite residual");
+      st->residual_mode = 3;
       done = res < update_margin * c->cfg.residual_tol;
+      how = "updated";
     }
     if (c->cfg.verbose)
-      std::printf("defect correction step %lld: max ||b - (I+A)x|| = %.3e (%s)\n", (long long)step + 1, res,
-                  (step == 0 || c->cfg.fp64_every_step) ? "FP64 operator" : "updated");
-  }
-  if (c->cfg.verify_residual) {
-    res = fp64_residual(c, b, x, nset, r, st);
-    done = res < c->cfg.residual_tol;
-    if (c->cfg.verbose) std::printf("verified: max ||b - (I+A)x|| = %.3e\n", res);
+      std::printf("defect correction step %lld: max ||b - (I+A)x|| = %.3e (%s, mode %lld)\n", (long long)step + 1,
+                  res, how, (long long)st->residual_mode);
   }
   st->residual_max = res;
   return done;

@@ -32,7 +32,7 @@ extern "C" cphf_status cphf_rij_response_bra_noalloc(const double* Z, const doub
                                                      int64_t nocc, int64_t naux, int64_t nb, double scale_j,
                                                      double* out, void* stream) {
   if (!Z || !bra || !out || nao <= 0 || nocc <= 0 || naux <= 0 || nb < 0) return CPHF_ERR_ARG;
-  if (naux * nb > kScratchElems) return CPHF_ERR_ARG;  // beyond the static scratch: see the header
+  if (nb > kScratchElems / naux) return CPHF_ERR_ARG;  // naux * nb beyond the static scratch (no overflow)
   if (nb == 0) return CPHF_OK;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {

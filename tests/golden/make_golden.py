@@ -1,8 +1,8 @@
 """Generate the golden vectors under tests/golden/ from the reference's own Python code.
 
-Run in a container where the reference project is mounted (default path below, or the
-``CPHF_REFERENCE`` environment variable).  Nothing at test time reads the reference: the
-tests only load the ``.npz`` files written here.
+Run where the reference project is available and name its root in the ``CPHF_REFERENCE``
+environment variable.  Nothing at test time reads the reference: the tests only load the
+``.npz`` files written here.
 
 What runs, all from the reference's sources:
 
@@ -17,8 +17,16 @@ What runs, all from the reference's sources:
 * ``pyhessref/hess_scf_restricted.RHessSCF`` and ``hess_scf_unrestricted.UHessSCF``
   (``response_dimless_cphf``, ``solve_dimless_cphf``, ``finalize_cphf``,
   ``get_cphf_hess``) driven by those naive plugins.
+* ``pyhessref/nimatmul/rks.get_ks_response_bra_naive`` and
+  ``pyhessref/nimatmul/uks.get_uks_response_bra_naive`` (the XC response in bra form) on seeded
+  synthetic grids: the stub ``pyscf.dft.numint.NumInt`` supplies the LDA fxc integral PySCF
+  would compute, ``nr_rks_fxc`` -> ``v1 = phi^T diag(w f rho1[dm1]) phi`` and ``nr_uks_fxc`` ->
+  ``v1_t = phi^T diag(w sum_s f[., s, t] rho1[dm1_s]) phi``, with ``rho1[dm] = sum phi dm phi``.
+  What runs from the reference is its wrapper: the perturbed density built from the bra
+  (``2 bra mocc^T`` for RKS, ``bra mocc^T`` per spin for UKS), its symmetrisation and the
+  projection ``v1 @ mocc``; the fxc integral itself is the stub's.
 
-Usage: ``python tests/golden/make_golden.py``
+Usage: ``CPHF_REFERENCE=<reference root> python tests/golden/make_golden.py``
 """
 
 import importlib.util
@@ -31,7 +39,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parent.parent
-REF = Path(os.environ.get("CPHF_REFERENCE", "/root/reference"))
+REF = Path(os.environ["CPHF_REFERENCE"]) if os.environ.get("CPHF_REFERENCE") else None
 sys.path.insert(0, str(REPO / "rstsr-showcase-hessian_gb300"))
 
 from cphf_gb300 import synth  # noqa: E402
@@ -63,10 +71,46 @@ def _install_stub_pyscf():
         return lambda: _CURRENT["int3c2e"]
 
     rhf._int3c_wrapper = _int3c_wrapper
-    pyscf.gto, pyscf.df, df.grad, grad.rhf = gto, df, grad, rhf
+    dft = types.ModuleType("pyscf.dft")
+    numint = types.ModuleType("pyscf.dft.numint")
+    numint.NumInt = _StubNumInt
+    dft.numint = numint
+    pyscf.gto, pyscf.df, df.grad, grad.rhf, pyscf.dft = gto, df, grad, rhf, dft
     for name, mod in {"pyscf": pyscf, "pyscf.gto": gto, "pyscf.df": df, "pyscf.df.grad": grad,
-                      "pyscf.df.grad.rhf": rhf}.items():
+                      "pyscf.df.grad.rhf": rhf, "pyscf.dft": dft, "pyscf.dft.numint": numint}.items():
         sys.modules[name] = mod
+
+
+def _rho1(ao, dm):
+    """rho1[p, g] = sum_{mu nu} ao[g, mu] dm[p, mu, nu] ao[g, nu] for dm [nprop, nao, nao]."""
+    return np.einsum("gu,puv,gv->pg", ao, dm, ao, optimize=True)
+
+
+def _fxc_mat(ao, wv):
+    """v[p] = ao^T diag(wv[p]) ao."""
+    return np.einsum("gu,pg,gv->puv", ao, wv, ao, optimize=True)
+
+
+class _StubNumInt:
+    """LDA fxc integrals on the synthetic grid of ``_CURRENT["grid"]`` (ao, weights, fxc)."""
+
+    def nr_rks_fxc(self, mol, grids, xc, dm0, dm1, hermi=1, rho0=None, vxc=None, fxc=None):
+        g = _CURRENT["grid"]
+        dm1 = np.asarray(dm1)
+        shape = dm1.shape
+        dm = dm1.reshape(-1, shape[-2], shape[-1])
+        wv = g.weights[None, :] * g.fxc[None, :] * _rho1(g.ao, dm)
+        return _fxc_mat(g.ao, wv).reshape(shape)
+
+    def nr_uks_fxc(self, mol, grids, xc, dm0, dm1, hermi=1, rho0=None, vxc=None, fxc=None):
+        g = _CURRENT["grid"]
+        dms = [np.asarray(d) for d in dm1]
+        rho = [_rho1(g.ao, d.reshape(-1, d.shape[-2], d.shape[-1])) for d in dms]
+        out = []
+        for t in range(2):
+            wv = g.weights[None, :] * (g.fxc[None, :, 0, t] * rho[0] + g.fxc[None, :, 1, t] * rho[1])
+            out.append(_fxc_mat(g.ao, wv).reshape(dms[t].shape))
+        return out
 
 
 class _FakeAux:
@@ -201,14 +245,53 @@ def uhf_golden(dims, tag, seed):
     np.savez(HERE / f"{tag}_seed{seed}.npz", **out)
 
 
+XC_RKS = dict(nao=30, naux=90, nocc=(6,), natm=3, decay=6.0, grid=True, points=(150, 260), window=12)
+XC_UKS = dict(nao=28, naux=84, nocc=(6, 5), natm=3, decay=6.0, grid=True, points=(140, 240), window=12)
+
+
+def xc_golden(dims, tag, seed):
+    """The reference's XC response wrappers (bra form) on a seeded synthetic grid."""
+    from pyhessref.nimatmul.rks import get_ks_response_bra_naive
+    from pyhessref.nimatmul.uks import get_uks_response_bra_naive
+
+    s = synth.make_system(dims, seed=seed)
+    g = s.grid
+    _CURRENT["grid"] = g
+    mol = _FakeMol(s.nao, s.natm)
+    rng = np.random.default_rng(seed + 300)
+    nprop = 4
+    out = dict(ao=g.ao, weights=g.weights, fxc=g.fxc, atom_offsets=g.atom_offsets, cderi=s.cderi,
+               scale_j=s.scale_j, scale_k=s.scale_k, nspin=s.nspin)
+    # bra [nao, nocc, nprop] (col-major meaning) <-> pyhessref's [nprop, nao, nocc]
+    if s.nspin == 1:
+        C, occ = s.mo_coeff[0], s.mo_occ[0]
+        bra = rng.standard_normal((s.nao, s.nocc[0], nprop))
+        resp = get_ks_response_bra_naive(mol, None, "lda", C, occ, None,
+                                         np.ascontiguousarray(np.transpose(bra, (2, 0, 1))))
+        out.update(mo_coeff0=C, mo_occ0=occ, mo_energy0=s.mo_energy[0], bra0=bra,
+                   resp0=np.asfortranarray(np.transpose(resp, (1, 2, 0))))
+    else:
+        bra = [rng.standard_normal((s.nao, s.nocc[t], nprop)) for t in range(2)]
+        resp = get_uks_response_bra_naive(mol, None, "lda", [c for c in s.mo_coeff], [o for o in s.mo_occ],
+                                          None, None,
+                                          [np.ascontiguousarray(np.transpose(b, (2, 0, 1))) for b in bra])
+        for t in range(2):
+            out.update({f"mo_coeff{t}": s.mo_coeff[t], f"mo_occ{t}": s.mo_occ[t],
+                        f"mo_energy{t}": s.mo_energy[t], f"bra{t}": bra[t],
+                        f"resp{t}": np.asfortranarray(np.transpose(resp[t], (1, 2, 0)))})
+    np.savez(HERE / f"{tag}_seed{seed}.npz", **out)
+
+
 def main():
-    if not (REF / "pyhessref").is_dir():
-        raise SystemExit(f"reference not found at {REF}")
+    if REF is None or not (REF / "pyhessref").is_dir():
+        raise SystemExit("set CPHF_REFERENCE to the reference project's root (the directory holding pyhessref/)")
     _install_stub_pyscf()
     sys.path.insert(0, str(REF))
     krylov_golden()
     rhf_golden("rhf_nao24", seed=1)
     uhf_golden(dict(nao=20, naux=70, nocc=(5, 4), natm=3, decay=6.0), "uhf_nao20", seed=2)
+    xc_golden(XC_RKS, "xc_rks_nao30", seed=3)
+    xc_golden(XC_UKS, "xc_uks_nao28", seed=4)
     print("golden vectors written to", HERE)
 
 

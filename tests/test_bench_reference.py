@@ -20,6 +20,7 @@ def test_reference_arm_json_line():
               "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
         assert k in d, k
     assert d["impl"] == "reference" and d["steps"] == 2 and d["warmup"] == 3
+    assert d["extrapolated"] is True and d["measured_step_s"] > 0
     assert d["value"] > 0 and d["higher_is_better"] is False
     assert d["config"]["workload"] == "rhf_nao24"
     cb = d["cpu_baseline"]

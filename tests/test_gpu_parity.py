@@ -219,6 +219,7 @@ def test_lowp_operator_accuracy(dims, tc):
     s = synth.make_system(dims, seed=14)
     c64 = make_ctx(s)
     clp = make_ctx(s, precision="mixed", tensor_cores=tc)
+    clp.profile(True)
     rng = np.random.default_rng(14)
     if s.nspin == 1:
         mo1 = rng.standard_normal((s.nao, s.nocc[0], 5))
@@ -228,6 +229,23 @@ def test_lowp_operator_accuracy(dims, tc):
         ref, got = c64.response_dimless_cphf(mo1), clp.response_dimless_cphf_lowp(mo1)
     for a, b in zip(got, ref):
         assert rel_err(a, b) < LOWP_TOL
+    if tc:
+        classes = ["kterm_tcgen05_f16x3", "tgen_tcgen05_f16x3", "wgen_tcgen05_f16x3", "term2_tcgen05_f16x3"]
+        if s.grid is not None:
+            classes.append("xc_tcgen05_f16x3")
+        assert_tensor_core_classes(clp, classes)
+    else:
+        assert not clp.tensor_cores_active
+        assert "kterm_tcgen05_f16x3" not in clp.profile_report()
+
+
+def assert_tensor_core_classes(ctx, classes):
+    """The context ran its split-precision / exact-slice contractions on tcgen05: the tensor
+    cores are active and each named kernel class of the CUDA-event profiler has launches."""
+    assert ctx.tensor_cores_active
+    rep = ctx.profile_report()
+    for name in classes:
+        assert rep.get(name, {}).get("launches", 0) > 0, (name, sorted(rep))
 
 
 def _max_col_residual(c64, s, x):
@@ -253,8 +271,15 @@ def test_emulated_fp64_residual(dims, mode):
     c64 = make_ctx(s)
     cmx = make_ctx(s, precision="mixed", residual_dfloat=mode, max_refine=1, residual_tol=1.0, verify_residual=0,
                    aux_chunk=16)
+    cmx.profile(True)
     x = cmx.solve_dimless_cphf(rhs)
     res_emul = cmx.last_stats["residual_max"]
+    assert cmx.last_stats["residual_mode"] == mode
+    if mode == 2:
+        classes = ["kterm_tcgen05_bf16x6_exact"]
+        if s.grid is not None:
+            classes.append("xc_tcgen05_bf16x6_exact")
+        assert_tensor_core_classes(cmx, classes)
     res_64, xmax = _max_col_residual(c64, s, x)
     assert 1e-9 < res_64 < 1e-3            # a real, unconverged residual of the low-precision step
     assert abs(res_emul - res_64) < 1e-9 * max(1.0, xmax), (res_emul, res_64, xmax)
@@ -268,12 +293,20 @@ def test_mixed_precision_solve(dims, dfloat):
     c64 = make_ctx(s, cphf_tol=1e-10, cphf_lindep=1e-20)
     x64 = c64.solve_dimless_cphf(rhs)
     cmx = make_ctx(s, precision="mixed", residual_dfloat=dfloat)
+    cmx.profile(dfloat == 2)
     xmx = cmx.solve_dimless_cphf(rhs)
     st = cmx.last_stats
     assert st["residual_max"] < 1e-8
     assert st["refine_steps"] >= 1 and st["lowp_matvec_columns"] > 0
     nset = 3 * s.natm
-    assert st["fp64_matvec_columns"] == 2 * nset   # first correction + final verification
+    # every correction's residual is recomputed with the FP64-accurate operator (the solve's own
+    # final check, verify_residual = 2); convergence is decided on that recomputed residual
+    assert st["fp64_matvec_columns"] == st["refine_steps"] * nset
+    assert st["residual_mode"] == dfloat
+    if dfloat == 2:
+        assert_tensor_core_classes(cmx, ["kterm_tcgen05_f16x3", "kterm_tcgen05_bf16x6_exact"])
+    res64, _ = _max_col_residual(c64, s, xmx)
+    assert res64 < 1e-8
     if s.nspin == 1:
         x64, xmx = [x64], [xmx]
     for a, b in zip(xmx, x64):
@@ -355,3 +388,81 @@ def test_empty_and_single_column(med):
     assert zero.shape == (s.nao, s.nocc[0], 0)
     x = ctx.solve_dimless_cphf(np.zeros((s.nao, s.nocc[0], 2)))
     assert np.all(x == 0.0)
+
+
+@pytest.mark.parametrize("name", ["xc_rks_nao30_seed3.npz", "xc_uks_nao28_seed4.npz"])
+def test_xc_plugin_matches_reference_wrapper_golden(name):
+    """The XC plugin (FP64 grouped kernels, and the mixed context's split-precision operator)
+    against the reference's own XC response wrappers (get_ks_response_bra_naive /
+    get_uks_response_bra_naive, tests/golden/make_golden.py)."""
+    g = load_golden(name)
+    nspin = int(g["nspin"])
+    C = [g[f"mo_coeff{t}"] for t in range(nspin)]
+    occ = [g[f"mo_occ{t}"] for t in range(nspin)]
+    e = [g[f"mo_energy{t}"] for t in range(nspin)]
+    bra = [g[f"bra{t}"] for t in range(nspin)]
+    ref = [g[f"resp{t}"] for t in range(nspin)]
+    arg = (lambda v: v[0]) if nspin == 1 else (lambda v: v)
+    for with_rijk in (False, True):
+        ctx = Context()
+        if with_rijk:
+            ctx.set_cderi(g["cderi"], float(g["scale_j"]), float(g["scale_k"]))
+        else:
+            ctx.set_nao(C[0].shape[0])
+        ctx.set_grid(g["ao"], g["weights"], g["fxc"], nspin, g["atom_offsets"])
+        ctx.make_response_preparation(arg(C), arg(occ), arg(e))
+        got = ctx.get_response_bra(arg(bra), plugin="xc")
+        got = [got] if nspin == 1 else got
+        for a, b in zip(got, ref):
+            assert rel_err(a, b) < 1e-12
+
+
+def test_fp64_operator_matches_oracle_at_nao600():
+    """The FP64 dimensionless operator at nao=600 / naux=2000 / nocc=60 (the 180-RHS workload),
+    on a few columns, against the CPU oracle's response_dimless_cphf: 1e-12 relative."""
+    s = synth.make_system("rhf_nao600", seed=0)
+    ctx = make_ctx(s)
+    drv = oracle_driver(s)
+    mo1 = np.random.default_rng(600).standard_normal((s.nao, s.nocc[0], 3))
+    assert rel_err(ctx.response_dimless_cphf(mo1), drv.response_dimless_cphf(mo1)) < 1e-12
+    bra = np.random.default_rng(601).standard_normal((s.nao, s.nocc[0], 2))
+    ref = rijk.rhf_response_bra(s.cderi, s.mo_coeff[0], s.mo_occ[0], bra, s.scale_j, s.scale_k)
+    assert rel_err(ctx.get_response_bra(bra), ref) < 1e-12
+
+
+def _bad_weights():
+    """MLP weights whose outputs are far off: a guess x0 = b (1 + o1) several times too large and
+    preconditioner entries m = 1 / (1 + o2) spread over two orders of magnitude."""
+    from oracle import mlp as omlp
+    d = omlp.unpack(omlp.init_weights(3).astype(np.float64))
+    d["W3"] = 3.0 * np.random.default_rng(33).standard_normal(d["W3"].shape)
+    d["b3"] = np.array([5.0, 30.0])
+    return omlp.pack(d).astype(np.float32)
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_mixed_solve_with_bad_learned_preconditioner(mode):
+    """A deliberately bad network costs iterations, never accuracy: the mixed solve's outer
+    FP64-accurate residual still decides convergence to ||b - (I+A)x|| < 1e-8."""
+    s = synth.make_system(MEDIUM, seed=31)
+    c64 = make_ctx(s)
+    cmx = make_ctx(s, precision="mixed", use_learned_guess=mode)
+    cmx.set_mlp_weights(_bad_weights())
+    x = cmx.solve_dimless_cphf(s.rhs[0])
+    assert cmx.last_stats["residual_max"] < 1e-8
+    res64, _ = _max_col_residual(c64, s, x)
+    assert res64 < 1e-8
+
+
+def test_fp64_solve_with_bad_learned_guess():
+    """On an FP64 context the network only supplies x0; the Krylov iteration and its stopping test
+    are the reference's, so a bad guess still converges to the plain solution."""
+    s = synth.make_system(MEDIUM, seed=32)
+    base = make_ctx(s, cphf_tol=1e-10)
+    x_ref = base.solve_dimless_cphf(s.rhs[0])
+    bad = make_ctx(s, cphf_tol=1e-10, use_learned_guess=1)
+    bad.set_mlp_weights(_bad_weights())
+    x = bad.solve_dimless_cphf(s.rhs[0])
+    assert np.abs(x[s.nocc[0]:] - x_ref[s.nocc[0]:]).max() < 1e-8
+    res64, _ = _max_col_residual(base, s, x)
+    assert res64 < 1e-8

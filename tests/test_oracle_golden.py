@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from conftest import load_golden, rel_err
-from oracle import cphf, krylov, rijk
+from oracle import cphf, krylov, rijk, xc
 
 
 @pytest.fixture(scope="module")
@@ -123,3 +123,60 @@ def test_cphf_nonconvergence_raises(rg):
     drv.config["cphf_max_cycle"] = 1
     with pytest.raises(krylov.KrylovNotConverged):
         drv.solve_dimless_cphf(rg["rhs"])
+
+
+# ---------------------------------------------------------------- XC response (bra form)
+def _xc_golden(name):
+    g = load_golden(name)
+    nspin = int(g["nspin"])
+    mocc = [g[f"mo_coeff{t}"][:, g[f"mo_occ{t}"] > 0] for t in range(nspin)]
+    return g, nspin, mocc
+
+
+def test_xc_rks_response_matches_reference_wrapper():
+    """oracle/xc.py against pyhessref/nimatmul/rks.py:get_ks_response_bra_naive (its 2 bra mocc^T
+    perturbed density, symmetrisation and v1 @ mocc; the stubbed NumInt gives the LDA fxc integral)."""
+    g, _, mocc = _xc_golden("xc_rks_nao30_seed3.npz")
+    got = xc.rks_response_bra(g["ao"], g["weights"], g["fxc"], g["bra0"], mocc[0])
+    assert rel_err(got, g["resp0"]) < 1e-12
+    got_b = xc.rks_response_bra(g["ao"], g["weights"], g["fxc"], g["bra0"], mocc[0], nbatch=3)
+    assert rel_err(got_b, g["resp0"]) < 1e-12
+
+
+def test_xc_uks_response_matches_reference_wrapper():
+    """oracle/xc.py against pyhessref/nimatmul/uks.py:get_uks_response_bra_naive (per-spin bra mocc^T
+    densities, spin-coupled fxc, v1_t @ mocc_t)."""
+    g, _, mocc = _xc_golden("xc_uks_nao28_seed4.npz")
+    got = xc.uks_response_bra(g["ao"], g["weights"], g["fxc"], [g["bra0"], g["bra1"]], mocc)
+    for t in range(2):
+        assert rel_err(got[t], g[f"resp{t}"]) < 1e-12
+
+
+# ---------------------------------------------------------------- j2c decomposition
+def test_j2c_recoverable_reference_case():
+    """pure_decompose.rs:333-356 (test_check_recoverable): U^T U reproduces the 3 x 3 metric."""
+    from oracle import decompose
+    j2c = np.array([[10.0, 1.0, 2.0], [1.0, 20.0, 3.0], [2.0, 3.0, 30.0]])
+    U, fallback = decompose.decomp_j2c_cd(j2c, None)
+    assert not fallback and np.allclose(U.T @ U, j2c, rtol=1e-12, atol=1e-12)
+    assert np.allclose(np.tril(U, -1), 0.0)
+    U2, fallback2 = decompose.decomp_j2c_cd(j2c, 1e-14)
+    assert not fallback2 and np.array_equal(U, U2)
+
+
+def test_j2c_eigenvalue_fallback_and_solve():
+    """The clamped-eigenvalue fallback (pure_decompose.rs:44-51) on an indefinite metric, and
+    cderi = j3c U^-1 (pure_decompose.rs:205-252)."""
+    from oracle import decompose
+    rng = np.random.default_rng(5)
+    q, _ = np.linalg.qr(rng.standard_normal((30, 30)))
+    e = np.linspace(-0.2, 3.0, 30)
+    j2c = (q * e) @ q.T
+    U, fallback = decompose.decomp_j2c_cd(j2c, 1e-3)
+    assert fallback
+    assert np.allclose(U.T @ U, (q * np.maximum(e, 1e-3)) @ q.T, atol=1e-12)
+    with pytest.raises(np.linalg.LinAlgError):
+        decompose.decomp_j2c_cd(j2c, None)
+    j3c = rng.standard_normal((50, 30))
+    cd = decompose.solve_by_j2c_right(j3c, U)
+    assert np.allclose(cd @ U, j3c, atol=1e-12)
