@@ -597,8 +597,15 @@ def run_gpu(args, world, rank, local):
         "kterm_tcgen05_bf16x6_exact": "exact BF16 slices, the tensor pipe executes 21 slice products",
         "xc_tcgen05_f16x3": "per grid batch over its AO window, FP16 hi/lo, 3 split products",
         "xc_tcgen05_bf16x6_exact": "per grid batch over its AO window, exact BF16 slices, 21 slice products",
+        "tgen_tcgen05_bf16x6_exact": "exact BF16 slices, the tensor pipe executes 21 slice products",
+        "wgen_tcgen05_bf16x6_exact": "exact BF16 slices, the tensor pipe executes 21 slice products",
+        "term2_tcgen05_bf16x6_exact": "exact BF16 slices, the tensor pipe executes 21 slice products",
+        "kterm_tcgen05_bf16x4c_exact": "exact BF16 slices in correction precision, 10 slice products",
+        "tgen_tcgen05_bf16x4c_exact": "exact BF16 slices in correction precision, 10 slice products",
+        "wgen_tcgen05_bf16x4c_exact": "exact BF16 slices in correction precision, 10 slice products",
+        "term2_tcgen05_bf16x4c_exact": "exact BF16 slices in correction precision, 10 slice products",
     }
-    if dom_name == "slice_scale_split":
+    if dom_name in ("slice_scale_split", "slice_exact"):
         roof = dict(bound="hbm", achieved=dom["bytes"] / dom["ms"] / 1e6, peak=hbm, unit="GB/s",
                     peak_source=f"{peak_src} HBM copy; achieved counts the algorithmic bytes (operands read, "
                                 "slice planes written) of the slicing / scaling kernels")
@@ -625,7 +632,10 @@ def run_gpu(args, world, rank, local):
     # products the tensor pipe executes per algorithmic FLOP (slices x slices kept)
     products = {"kterm_tcgen05_f16x3": 3, "tgen_tcgen05_f16x3": 3, "wgen_tcgen05_f16x3": 3,
                 "term2_tcgen05_f16x3": 3, "kterm_tcgen05_bf16x6_exact": 21,
-                "xc_tcgen05_f16x3": 3, "xc_tcgen05_bf16x6_exact": 21}.get(dom_name)
+                "xc_tcgen05_f16x3": 3, "xc_tcgen05_bf16x6_exact": 21, "tgen_tcgen05_bf16x6_exact": 21,
+                "wgen_tcgen05_bf16x6_exact": 21, "term2_tcgen05_bf16x6_exact": 21,
+                "kterm_tcgen05_bf16x4c_exact": 10, "tgen_tcgen05_bf16x4c_exact": 10,
+                "wgen_tcgen05_bf16x4c_exact": 10, "term2_tcgen05_bf16x4c_exact": 10}.get(dom_name)
     if products and roof.get("peak"):
         roof.update(tensor_executed_tflops=roof["achieved"] * products,
                     tensor_executed_frac=roof["achieved"] * products / roof["peak"])

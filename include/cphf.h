@@ -71,9 +71,12 @@ typedef struct cphf_config {
   int32_t verify_residual;   /* mixed: how the residual of every correction after the first is obtained and
                                 convergence decided.  0 = updated with the split-precision operator,
                                 r -= (I + A_lowp) d (no FP64-accurate application);  1 = recomputed with
-                                the native FP64 operator;  2 = recomputed with the FP64-accurate operator
-                                selected by residual_dfloat (default).  With 1 or 2 the solve returns only
-                                after a recomputed max_j ||b_j - (I+A)x_j||_2 < residual_tol. */
+                                the native FP64 operator;  2 (default) = computed with the FP64-accurate
+                                operator of residual_dfloat: with the exact-slice tensor cores (residual_dfloat
+                                = 2) as r -= (I + A) d, the correction d applied in correction precision
+                                (4 BF16 slices per operand, 10 exact-accumulated products, ~2^-24 relative
+                                to |d| where |d| ~ inner_tol |r|), otherwise recomputed in full.  With 1 or 2
+                                the solve returns only after such a max_j ||b_j - (I+A)x_j||_2 < residual_tol. */
   int32_t fp64_every_step;   /* mixed: FP64 residual after every correction, not only the first (default 0) */
   int64_t xc_chunk_points;   /* grid points per XC chunk (default 0 = 8 GiB of intermediates) */
   int32_t residual_dfloat;   /* mixed: arithmetic of the correction residuals.  0 = native FP64;
@@ -101,7 +104,9 @@ typedef struct cphf_stats {
   double seconds;               /* wall time of the call */
   int64_t residual_mode;        /* how residual_max was computed: 0 native FP64, 1 double-float GEMMs,
                                    2 double-float + exact BF16 slice products on the tensor cores,
-                                   3 updated with the split-precision operator, -1 not computed */
+                                   3 updated with the split-precision operator, 4 as 2 for the first
+                                   correction, later corrections subtracted with the exact-slice operator
+                                   in correction precision, -1 not computed */
 } cphf_stats;
 
 typedef struct cphf_ctx cphf_ctx;
@@ -225,6 +230,16 @@ cphf_status cphf_response_dimless_lowp(cphf_ctx* ctx, const double* const* mo1, 
  * MIXED: the same solver on the split-precision operator inside FP64 defect correction. */
 cphf_status cphf_solve_dimless_cphf(cphf_ctx* ctx, const double* const* rhs, int64_t nprop,
                                     const double* const* x0, double* const* mo1, cphf_stats* stats);
+/* compute_dimless_cphf_rhs (rscf.rs:104-182, uscf.rs:78-173) from the summed skeleton
+ * derivatives of the providers:  f1ao_core [nao, nao, 3, natm] (core-Hamiltonian derivatives,
+ * spin independent; NULL = 0), f1bra_el[s] [nao, nocc_s, 3, natm] (the electron-interaction
+ * plugins' get_deriv1_bra, half-transformed; NULL or a NULL entry = 0), s1ao [nao, nao, 3, natm]
+ * (overlap derivatives).  Out, per spin, [nmo, nocc_s, 3, natm]: rhs (vir: -(f1mo - s1mo e_i) /
+ * (e_a - e_i + level_shift); occ: -0.5 s1mo), f1mo = C^T (f1ao_core Cocc + f1bra_el),
+ * s1mo = C^T s1ao Cocc.  FP64. */
+cphf_status cphf_compute_dimless_cphf_rhs(cphf_ctx* ctx, const double* f1ao_core, const double* const* f1bra_el,
+                                          const double* s1ao, int64_t natm, double* const* rhs, double* const* f1mo,
+                                          double* const* s1mo);
 /* finalize_cphf (rscf.rs:328-353, uscf.rs:365-406): f1mo[s], s1mo[s] [nmo, nocc_s, 3, natm];
  * mo1[s] in/out; mo_e1[s] [nocc_s, nocc_s, 3, natm] out.  Its one response_mo (rscf.rs:342)
  * runs in native FP64 on an FP64 context and in the FP64-accurate arithmetic selected by

@@ -10,6 +10,9 @@ Restates the CPHF part of ``src/hessian/rscf.rs`` and ``src/hessian/uscf.rs``:
 * ``RHF.get_cphf_hess``          -- ``rscf.rs:371-399``
 * ``UHF.*``                      -- ``uscf.rs:203-446`` (both spins concatenated
   into one Krylov vector per column, ``uscf.rs:292-334``)
+* :func:`compute_dimless_cphf_rhs` -- ``rscf.rs:104-182`` (RHF) and ``uscf.rs:78-173``
+  (UHF, per spin with the shared core and overlap derivatives), from the summed skeleton
+  derivatives the core / electron-interaction / overlap providers return
 
 Electron-interaction plugins are callables ``get_response_bra(bra) -> resp``
 (RHF: ``[nao, nocc, nprop]``; UHF: two-spin lists), mirroring
@@ -202,3 +205,33 @@ def _cphf_hess(spins, factors, natm):
         for B in range(A):
             de[:, :, A, B] += de[:, :, B, A].T
     return de
+
+
+def compute_dimless_cphf_rhs(mo_coeff, mo_occ, mo_energy, f1ao_core, f1bra_el, s1ao, level_shift=0.0):
+    """``compute_dimless_cphf_rhs`` (rscf.rs:104-182; uscf.rs:78-173 per spin).
+
+    ``f1ao_core``, ``s1ao``: ``[nao, nao, 3, natm]`` (``f1ao_core`` may be None = 0);
+    ``f1bra_el``: ``[nao, nocc, 3, natm]`` (None = 0).  Returns ``(rhs, f1mo, s1mo)``, each
+    ``[nmo, nocc, 3, natm]``."""
+    C = np.asarray(mo_coeff, dtype=np.float64)
+    occ = np.asarray(mo_occ) > 0
+    no = int(occ.sum())
+    mocc = C[:, occ]
+    e = np.asarray(mo_energy, dtype=np.float64)
+    eocc, evir = e[occ], e[~occ]
+    e_ai_shift = evir[:, None] - eocc[None, :] + level_shift
+    s1ao = np.asarray(s1ao)
+    nao = C.shape[0]
+    tail = s1ao.shape[2:]
+    f1bra = np.zeros((nao, no) + tail)
+    if f1ao_core is not None:
+        f1bra += np.einsum("uvxA,vi->uixA", f1ao_core, mocc, optimize=True)     # f1ao_core % mocc
+    if f1bra_el is not None:
+        f1bra += f1bra_el
+    f1mo = np.einsum("up,uixA->pixA", C, f1bra, optimize=True)                 # mo_coeff^T % f1bra
+    s1mo = np.einsum("up,uvxA,vi->pixA", C, s1ao, mocc, optimize=True)          # C^T (s1ao % mocc)
+    b1mo = f1mo - s1mo * eocc[None, :, None, None]
+    rhs = np.zeros_like(f1mo)
+    rhs[no:] = -b1mo[no:] / e_ai_shift[:, :, None, None]
+    rhs[:no] = -0.5 * s1mo[:no]
+    return rhs, f1mo, s1mo

@@ -38,6 +38,7 @@ EXPORTS = [
     "cphf_ctx_profile", "cphf_ctx_profile_report", "cphf_mlp_get_weights", "cphf_mlp_features",
     "cphf_mlp_forward", "cphf_mlp_loss_grad", "cphf_mlp_train", "cphf_rij_noalloc_capacity",
     "cphf_rij_response_bra_noalloc", "cphf_j2c_decompose", "cphf_rijk_set_j3c", "cphf_rijk_get_cderi",
+    "cphf_compute_dimless_cphf_rhs",
 ]
 MLP_NWEIGHTS = 4546
 
@@ -173,6 +174,7 @@ def load_library():
         "cphf_j2c_decompose": ([vp, vp, i64, dbl, vp, ctypes.POINTER(J2cInfo)], i32),
         "cphf_rijk_set_j3c": ([vp, vp, vp, i64, i64, dbl, dbl, dbl, ctypes.POINTER(J2cInfo)], i32),
         "cphf_rijk_get_cderi": ([vp, vp], i32),
+        "cphf_compute_dimless_cphf_rhs": ([vp, vp, pp, vp, i64, pp, pp, pp], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -454,6 +456,27 @@ class Context:
         self.last_stats = st.as_dict()
         self._check(status)
         return out if uhf else out[0]
+
+    def compute_dimless_cphf_rhs(self, f1ao_core, f1bra_el, s1ao):
+        """``compute_dimless_cphf_rhs`` (src/hessian/rscf.rs:104-182, uscf.rs:78-173): returns
+        ``(rhs, f1mo, s1mo)`` (RHF arrays or UHF two-spin lists) from the skeleton derivatives
+        ``f1ao_core`` / ``s1ao`` ``[nao, nao, 3, natm]`` and ``f1bra_el`` ``[nao, nocc_s, 3, natm]``
+        (per spin for UHF; ``f1ao_core`` / ``f1bra_el`` may be None)."""
+        if self.nspin is None:
+            raise CphfError(ERR_STATE, "make_response_preparation has not been called")
+        natm = int(np.prod(_shape(s1ao)[2:])) // 3
+        tail = tuple(_shape(s1ao)[2:])
+        el = None
+        if f1bra_el is not None:
+            el, _ = self._spins(f1bra_el)
+        outs = [[np.zeros((self.nmo, self.nocc[s]) + tail, order="F") for s in range(self.nspin)] for _ in range(3)]
+        k = _Keep()
+        self._check(self.lib.cphf_compute_dimless_cphf_rhs(
+            self.h, k.ptr(f1ao_core), k.ptrs(el) if el is not None else None, k.ptr(s1ao), natm,
+            k.ptrs(outs[0]), k.ptrs(outs[1]), k.ptrs(outs[2])))
+        if self.nspin == 1:
+            return tuple(o[0] for o in outs)
+        return tuple(outs)
 
     def finalize_cphf(self, f1mo, s1mo, mo1):
         """``finalize_cphf``: returns ``(mo1, mo_e1)``."""

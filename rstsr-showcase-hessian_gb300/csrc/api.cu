@@ -597,6 +597,61 @@ cphf_status cphf_solve_dimless_cphf(cphf_ctx* c, const double* const* rhs, int64
   return rc;
 }
 
+cphf_status cphf_compute_dimless_cphf_rhs(cphf_ctx* c, const double* f1ao_core, const double* const* f1bra_el,
+                                          const double* s1ao, int64_t natm, double* const* rhs, double* const* f1mo,
+                                          double* const* s1mo) {
+  return guarded(c, [&] {
+    CPHF_CHECK_ARG(c->nspin == 1 || c->nspin == 2, "cphf_prepare has not been called");
+    CPHF_CHECK_ARG(s1ao && rhs && f1mo && s1mo, "null arrays");
+    CPHF_CHECK_SHAPE(natm > 0, "natm must be positive");
+    const int64_t nao = c->nao, nprop = 3 * natm, nsq = nao * nao * nprop;
+    // shared AO derivatives (core Fock and overlap are spin independent, uscf.rs:104-148)
+    DevBuf ao;
+    ao.ensure((size_t)2 * nsq * 8, c->counter());
+    double* F = ao.as<double>();
+    double* S1 = F + nsq;
+    if (f1ao_core) copy_in(c, F, f1ao_core, (size_t)nsq * 8);
+    copy_in(c, S1, s1ao, (size_t)nsq * 8);
+    for (int s = 0; s < c->nspin; ++s) {
+      const SpinState& sp = c->spin[s];
+      const int64_t no = sp.nocc, nmo = sp.nmo, nb = nao * no * nprop, nm = nmo * no * nprop;
+      DevBuf tmp;
+      tmp.ensure((size_t)std::max<int64_t>(2 * nb + 3 * nm, 1) * 8, c->counter());
+      double* fbra = tmp.as<double>();
+      double* sbra = fbra + nb;
+      double* f1 = sbra + nb;
+      double* s1 = f1 + nm;
+      double* r = s1 + nm;
+      if (f1bra_el && f1bra_el[s]) copy_in(c, fbra, f1bra_el[s], (size_t)nb * 8);
+      else CPHF_CUDA(cudaMemsetAsync(fbra, 0, (size_t)nb * 8, c->stream));
+      if (no > 0) {
+        GemmDesc g;  // f1bra = f1bra_el + f1ao_core Cocc   (rscf.rs:158), batched over the 3 natm derivatives
+        g.M = nao; g.N = no; g.K = nao; g.batch1 = nprop;
+        g.A = F; g.a_m = 1; g.a_k = nao; g.a_b1 = nao * nao;
+        g.B = sp.C.p; g.b_k = 1; g.b_n = nao; g.b_b1 = 0;
+        g.C = fbra; g.c_m = 1; g.c_n = nao; g.c_b1 = nao * no;
+        g.beta = 1.0;
+        if (f1ao_core) gemm64(c, g);
+        g.A = S1; g.C = sbra; g.beta = 0.0;  // s1ao Cocc   (rscf.rs:169)
+        gemm64(c, g);
+        GemmDesc m;  // f1mo = C^T f1bra, s1mo = C^T (s1ao Cocc)   (rscf.rs:159, 169)
+        m.M = nmo; m.N = no * nprop; m.K = nao;
+        m.A = sp.C.p; m.a_m = nao; m.a_k = 1;
+        m.B = fbra; m.b_k = 1; m.b_n = nao;
+        m.C = f1; m.c_m = 1; m.c_n = nmo;
+        gemm64(c, m);
+        m.B = sbra; m.C = s1;
+        gemm64(c, m);
+        launch_cphf_rhs(f1, s1, sp.e.as<double>(), nmo, no, nprop, c->cfg.level_shift, r, c->stream);
+      }
+      copy_out(c, rhs[s], r, (size_t)nm * 8);
+      copy_out(c, f1mo[s], f1, (size_t)nm * 8);
+      copy_out(c, s1mo[s], s1, (size_t)nm * 8);
+      CPHF_CUDA(cudaStreamSynchronize(c->stream));
+    }
+  });
+}
+
 cphf_status cphf_finalize_cphf(cphf_ctx* c, const double* const* f1mo, const double* const* s1mo,
                                int64_t natm, double* const* mo1, double* const* mo_e1) {
   return guarded(c, [&] {

@@ -77,6 +77,7 @@ struct LowpState {
   DevBuf s_c1, s_resp, s_T, s_W, s_d, s_ket, s_rho, s_y, s_x, s_Thi, s_Tlo, s_acc;
   DevBuf err;                  // device error flag of the tensor-core kernels (bounded waits)
   double sA = 1.0;             // power-of-two scale of the FP16 cderi planes
+  int64_t budget = int64_t(1) << 30;  // bytes per chunk of T / W intermediates (set at preparation)
   bool use_tc = true;
   // captured operator applications (cfg.cuda_graphs)
   std::vector<OpGraph> graphs;
@@ -175,7 +176,15 @@ enum ProfClass {
   PROF_TC_TERM2 = 11,
   PROF_XC_TC32 = 12,
   PROF_XC_TC64 = 13,
-  PROF_NCLASS = 14
+  PROF_OZ_TGEN = 14,
+  PROF_OZ_WGEN = 15,
+  PROF_OZ_TERM2 = 16,
+  PROF_OZC_KTERM = 17,
+  PROF_OZC_TGEN = 18,
+  PROF_OZC_WGEN = 19,
+  PROF_OZC_TERM2 = 20,
+  PROF_SLICE_EXACT = 21,
+  PROF_NCLASS = 22
 };
 extern const char* const kProfNames[PROF_NCLASS];
 
@@ -221,6 +230,7 @@ struct cphf_ctx {
   cphf::Profiler prof;
   bool f64_emulate = false;  // route the FP64 GEMMs through the double-float kernel
   bool oz_kterm = false;     // FP64 K term 1 on the tensor cores (exact BF16 slices)
+  bool oz_correction = false;  // ... in correction precision (slices 0-3, 10 products)
   bool oz_xc = false;        // FP64 XC response on the tensor cores (exact BF16 slices)
 
   int64_t* counter() { return &device_bytes; }
@@ -299,7 +309,7 @@ void lowp_release(cphf_ctx* c);
 struct AccurateScope {
   cphf_ctx* c;
   int used = 0;
-  AccurateScope(cphf_ctx* ctx, int mode);
+  AccurateScope(cphf_ctx* ctx, int mode, bool correction = false);
   ~AccurateScope();
   AccurateScope(const AccurateScope&) = delete;
   AccurateScope& operator=(const AccurateScope&) = delete;

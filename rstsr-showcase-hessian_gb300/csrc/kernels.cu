@@ -514,6 +514,21 @@ __global__ void finalize_kernel(const double* __restrict__ f1, const double* __r
   }
 }
 
+// compute_dimless_cphf_rhs element-wise part (src/hessian/rscf.rs:174-178):
+//   rhs[vir] = -(f1mo - s1mo e_i)[vir] / (e_a - e_i + shift),  rhs[occ] = -0.5 s1mo[occ]
+__global__ void cphf_rhs_kernel(const double* __restrict__ f1, const double* __restrict__ s1,
+                                const double* __restrict__ e, int64_t nmo, int64_t nocc, int64_t nprop, double shift,
+                                double* __restrict__ rhs) {
+  const int64_t per = nmo * nocc;
+  const int64_t total = per * nprop;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t % per;
+    const int64_t p = r % nmo, i = r / nmo;
+    rhs[t] = p >= nocc ? -(f1[t] - s1[t] * e[i]) / (e[p] - e[i] + shift) : -0.5 * s1[t];
+  }
+}
+
 __global__ void hess_pairs_kernel(const double* __restrict__ f1, const double* __restrict__ s1,
                                   const double* __restrict__ mo1, const double* __restrict__ mo_e1,
                                   const double* __restrict__ e, int64_t nmo, int64_t nocc, int64_t nprop,
@@ -562,6 +577,13 @@ void launch_finalize(const double* f1, const double* s1, const double* resp, con
                      int64_t nocc, int64_t nprop, double* mo1, double* mo_e1, cudaStream_t s) {
   if (nmo * nocc * nprop <= 0) return;
   finalize_kernel<<<grid_for(nmo * nocc * nprop), kThreads, 0, s>>>(f1, s1, resp, e, nmo, nocc, nprop, mo1, mo_e1);
+  count_launch();
+}
+
+void launch_cphf_rhs(const double* f1, const double* s1, const double* e, int64_t nmo, int64_t nocc, int64_t nprop,
+                     double shift, double* rhs, cudaStream_t s) {
+  if (nmo * nocc * nprop <= 0) return;
+  cphf_rhs_kernel<<<grid_for(nmo * nocc * nprop), kThreads, 0, s>>>(f1, s1, e, nmo, nocc, nprop, shift, rhs);
   count_launch();
 }
 

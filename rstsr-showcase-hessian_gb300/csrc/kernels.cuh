@@ -85,6 +85,12 @@ void launch_finalize(const double* f1, const double* s1, const double* resp, con
                      int64_t nmo, int64_t nocc, int64_t nprop, double* mo1, double* mo_e1,
                      cudaStream_t s);
 
+// compute_dimless_cphf_rhs element-wise part (src/hessian/rscf.rs:174-178):
+//   rhs[vir] = -(f1mo - s1mo e[i])[vir] / (e[a] - e[i] + shift),  rhs[occ] = -0.5 s1mo[occ]
+// f1mo, s1mo, rhs: [nmo, nocc, nprop].
+void launch_cphf_rhs(const double* f1, const double* s1, const double* e, int64_t nmo, int64_t nocc, int64_t nprop,
+                     double shift, double* rhs, cudaStream_t s);
+
 // get_cphf_hess pair sums (src/hessian/rscf.rs:378-388): G[r, q] += f0 <mo1_r, f1mo_q>
 // - f1 <mo1_r, s1mo_q eocc> - f2 <mo_e1_r, s1mo_q[occ]>, r, q over the nprop = 3 natm columns.
 void launch_hess_pairs(const double* f1, const double* s1, const double* mo1, const double* mo_e1,

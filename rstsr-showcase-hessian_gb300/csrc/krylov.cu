@@ -40,7 +40,9 @@ void orth_block(cphf_ctx* c, const KrylovWork& w, double* V, int64_t n, int64_t 
   if (m == 0) return;
   double* ipd = w.part + mgs_partials_size(n, m) + m;  // after partials + coef
   {
-    ProfScope ps(c, PROF_KRYLOV, 0.0, 0.0);
+    // algorithmic work of the right-looking MGS: m(m-1)/2 dot + axpy pairs of length n
+    // (~2 n m^2 FLOPs), each step re-reading and re-writing the trailing columns (~8 n m^2 bytes)
+    ProfScope ps(c, PROF_KRYLOV, 2.0 * n * m * m, 8.0 * n * m * m);
     launch_mgs(V, n, m, lindep, ipd, w.keep, w.part, c->stream);
   }
   CPHF_CUDA(cudaMemcpyAsync(keep.data(), w.keep, m * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -71,7 +73,8 @@ void projected_solve(cphf_ctx* c, const KrylovWork& w, int64_t n, int64_t nd, in
   g.C = w.gw; g.c_m = 1; g.c_n = nd;
   gemm64(c, g);
   {
-    ProfScope ps(c, PROF_KRYLOV, 0.0, 0.0);
+    // LU with partial pivoting (2/3 nd^3) and the forward / back substitutions (2 nd^2 nset)
+    ProfScope ps(c, PROF_KRYLOV, (2.0 / 3.0) * nd * nd * nd + 2.0 * nd * nd * nset, 8.0 * nd * (nd + nset));
     launch_lu_solve(w.hw, nd, w.gw, nd, nd, nset, w.info, c->stream);
   }
   int info = 0;

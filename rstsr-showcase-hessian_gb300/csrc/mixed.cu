@@ -62,6 +62,13 @@ void lowp_prepare(cphf_ctx* c) {
     L.phi32.ensure((size_t)std::max<int64_t>(tot, 1) * 4, c->counter());
     launch_to_f32(c->phi.as<double>(), tot, L.phi32.as<float>(), c->stream);
   }
+  // Chunk budget of the K term's T / W intermediates: up to 8 GiB, at most a quarter of the
+  // memory still free once the resident operand planes are in place (fewer, longer launches).
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+    L.budget = std::max<int64_t>(int64_t(256) << 20, std::min<int64_t>(int64_t(8) << 30, (int64_t)(free_b / 4)));
+  else
+    cudaGetLastError();
 }
 
 static int64_t k_chunk_lowp(const cphf_ctx* c, int64_t no, int64_t nb) {
@@ -127,8 +134,11 @@ static void rijk_response_lowp(cphf_ctx* c, float* const* bra, int64_t nb, float
                      lp_tgen_planes(c, L.lp, s, P0, npc, nb, L.ldk, hi, lo, mx, scale, (float)L.sA,
                                     (float)-c->scale_k, err);
                    });
-        for (int64_t P0 = 0; P0 < naux; P0 += np_max)
-          lp_w_term2(c, L.lp, s, P0, std::min<int64_t>(np_max, naux - P0), nb, -c->scale_k, out[s], err);
+        // W / term-2 chunk: FP32 W staging and its two FP16 planes, nocc-wide rows, within the budget
+        const int64_t ldj = (no + 7) / 8 * 8;
+        const int64_t np_w = std::max<int64_t>(1, std::min<int64_t>(naux, L.budget / std::max<int64_t>(8 * no * nb * ldj, 1)));
+        for (int64_t P0 = 0; P0 < naux; P0 += np_w)
+          lp_w_term2(c, L.lp, s, P0, std::min<int64_t>(np_w, naux - P0), nb, -c->scale_k, out[s], err);
         continue;
       }
       L.s_T.ensure((size_t)nao * np_max * no * nb * 4, c->counter());
@@ -333,11 +343,12 @@ void lowp_apply(cphf_ctx* c, const double* x, int64_t nb, double* y) {
   L.graphs.push_back(g);
 }
 
-AccurateScope::AccurateScope(cphf_ctx* ctx, int mode) : c(ctx) {
+AccurateScope::AccurateScope(cphf_ctx* ctx, int mode, bool correction) : c(ctx) {
   const bool tc = c->lowp && c->lowp->use_tc && oz_available(c);
   c->f64_emulate = mode != 0;
   c->oz_kterm = mode == 2 && c->has_rijk && tc && oz_supported(c);
   c->oz_xc = mode == 2 && c->has_xc && tc;
+  c->oz_correction = correction && c->oz_kterm;
   // mode 2 without any tensor-core contraction available is the double-float operator
   used = mode == 2 && !(c->oz_kterm || c->oz_xc) ? 1 : mode;
 }
@@ -346,6 +357,7 @@ AccurateScope::~AccurateScope() {
   c->f64_emulate = false;
   c->oz_kterm = false;
   c->oz_xc = false;
+  c->oz_correction = false;
 }
 
 bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, double* x, cphf_stats* st,
@@ -421,7 +433,29 @@ bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, d
     launch_axpby(1.0, dlt, 1.0, x, n * nset, s);
     st->refine_steps += 1;
     const char* how;
-    if (step == 0 || c->cfg.fp64_every_step || final_mode >= 0) {
+    if (step > 0 && c->cfg.verify_residual == 2 && first_mode == 2 && !c->cfg.fp64_every_step &&
+        st->residual_mode != 3) {
+      // r -= (I + A) d with the exact-slice operator in correction precision: d is a correction
+      // of relative size ~inner accuracy, so 4 BF16 slices per operand (10 exact-accumulated
+      // products, ~2^-24 relative to |d|) keep this term far below the recomputed residual's
+      // own ~2^-34 |x|; r stays a computed residual, not a split-precision estimate.
+      int used = 0;
+      {
+        AccurateScope scope(c, 2, true);
+        response_mo_fp64(c, dlt, nset, adl, true);
+        used = scope.used;
+      }
+      st->fp64_matvec_columns += nset;
+      launch_residual_norms(r, dlt, adl, r, n, nset, c->k_norm.as<double>(), c->k_norm.as<double>() + nset, s);
+      CPHF_CUDA(cudaMemcpyAsync(h.data(), c->k_norm.p, nset * 8, cudaMemcpyDeviceToHost, s));
+      CPHF_CUDA(cudaStreamSynchronize(s));
+      res = 0.0;
+      for (double v : h) res = std::max(res, std::sqrt(v));
+      if (!std::isfinite(res)) throw Error(CPHF_ERR_NONFINITE, "non-finite residual");
+      st->residual_mode = used == 2 ? 4 : used;
+      done = res < c->cfg.residual_tol;
+      how = "exact-slice correction update";
+    } else if (step == 0 || c->cfg.fp64_every_step || final_mode >= 0) {
       const int mode = (step == 0 || final_mode < 0) ? first_mode : final_mode;
       accurate_residual(mode);
       done = res < c->cfg.residual_tol;

@@ -28,7 +28,11 @@ const char* const kProfNames[PROF_NCLASS] = {"gemm_fp64_simt", "gemm_fp32_simt",
                                              "tgen_tcgen05_f16x3", "slice_scale_split",
                                              "krylov_mgs_lu", "xc_grouped_fp64", "xc_grouped_fp32",
                                              "wgen_tcgen05_f16x3", "term2_tcgen05_f16x3",
-                                             "xc_tcgen05_f16x3", "xc_tcgen05_bf16x6_exact"};
+                                             "xc_tcgen05_f16x3", "xc_tcgen05_bf16x6_exact",
+                                             "tgen_tcgen05_bf16x6_exact", "wgen_tcgen05_bf16x6_exact",
+                                             "term2_tcgen05_bf16x6_exact", "kterm_tcgen05_bf16x4c_exact",
+                                             "tgen_tcgen05_bf16x4c_exact", "wgen_tcgen05_bf16x4c_exact",
+                                             "term2_tcgen05_bf16x4c_exact", "slice_exact"};
 
 static double gemm_flops(const GemmDesc& d) { return 2.0 * d.M * d.N * d.K * d.batch1 * d.batch2; }
 
@@ -138,7 +142,7 @@ void rijk_response_fp64(cphf_ctx* c, const double* const* bra, int64_t nb, doubl
       if (c->oz_kterm && c->lowp) {
         if (!written[s]) CPHF_CUDA(cudaMemsetAsync(out[s], 0, (size_t)nao * no * nb * 8, c->stream));
         written[s] = true;
-        oz_k_terms(c, c->lowp->oz, s, bra[s], nb, -c->scale_k, out[s]);
+        oz_k_terms(c, c->lowp->oz, s, bra[s], nb, -c->scale_k, out[s], c->oz_correction);
         continue;
       }
       const int64_t np_max = k_chunk(c, no, nb);

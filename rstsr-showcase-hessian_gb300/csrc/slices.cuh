@@ -17,6 +17,15 @@ struct Exact6 {
   static constexpr bool BF16 = true;
   using Elem = __nv_bfloat16;
 };
+// The same exact BF16 slice planes read in correction precision: only slices 0-3 of each
+// operand and the 10 products with t + u <= 3 (dropped terms ~2^-24 relative to the row and
+// column maxima), for operators applied to a small correction whose result only has to be
+// accurate relative to the correction itself.  Same planes, same exact accumulation bounds.
+struct Exact6c {
+  static constexpr int S = 4, NACC = 4, EOFF = 0, STAGES = 3;
+  static constexpr bool BF16 = true;
+  using Elem = __nv_bfloat16;
+};
 struct Split2 {
   static constexpr int S = 2, NACC = 1, EOFF = 14, STAGES = 6;
   static constexpr bool BF16 = false;

@@ -304,8 +304,9 @@ void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, 
   LowpState& L = *c->lowp;
   const int64_t nao = c->nao, naux = c->naux;
   const int64_t N = no * nb;
-  // aux functions per chunk: T planes bounded by ~1 GiB, batched T generation within grid limits
-  int64_t np = std::max<int64_t>(1, (int64_t(1) << 30) / std::max<int64_t>(N * ldk * 4, 1));
+  // aux functions per chunk: both T planes within the context's chunk budget, batched T
+  // generation within grid limits
+  int64_t np = std::max<int64_t>(1, L.budget / std::max<int64_t>(N * ldk * 4, 1));
   np = std::min<int64_t>(np, std::max<int64_t>(1, 65535 / std::max<int64_t>(nb, 1)));
   np = std::min<int64_t>(np, naux);
   const size_t plane = (size_t)np * N * ldk * 2;

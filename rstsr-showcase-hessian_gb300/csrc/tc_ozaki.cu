@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(128, 1)
 template <class PR>
 struct Batched {
   static constexpr int BN = 64;
-  static constexpr int STAGES = PR::S == 6 ? 2 : 3;  // split FP16: small stages, 2-3 CTAs per SM
+  static constexpr int STAGES = PR::S == 6 ? 2 : 3;  // 6 exact slices: 2 stages; 4 slices / split FP16: 3
   static constexpr int THREADS = 320;
   static constexpr int EPI_WARPS = 8;
   static constexpr int SMEM_BYTES = STAGES * Cfg<PR, BN>::STAGE_BYTES + 1024 + 1024;
@@ -358,7 +358,7 @@ __device__ __forceinline__ float pow2f(int e) {
 enum { EPI_STORE = 0, EPI_SPLIT16 = 2 };
 
 template <class PR, int BN, int EPI = EPI_STORE>
-__global__ void __launch_bounds__(320, PR::S == 6 ? 1 : 2)
+__global__ void __launch_bounds__(320, PR::NACC == 4 ? 1 : 2)
     tc_slice_batched_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB,
                             OzArgs args) {
   using C = Cfg<PR, BN>;
@@ -723,7 +723,7 @@ CUtensorMap make_map(const void* base, int64_t K, int64_t rows, int64_t depth, i
 
 template <class PR, int BN>
 bool set_short_smem_attr() {
-  if constexpr (PR::S == 6) {
+  if constexpr (PR::NACC == 4) {
     return true;
   } else {
     return cudaFuncSetAttribute(tc_slice_kernel<PR, BN, SHORT_STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -738,7 +738,7 @@ bool set_smem_attr() {
          set_short_smem_attr<PR, BN>() &&
          cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               Batched<PR>::SMEM_BYTES) == cudaSuccess &&
-         (PR::S == 6 ||
+         (PR::NACC == 4 ||
           cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64, EPI_SPLIT16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                Batched<PR>::SMEM_BYTES) == cudaSuccess);
 }
@@ -890,7 +890,7 @@ bool oz_available(cphf_ctx* c) {
   static bool attr_ok = false, tried = false;
   if (!tried) {
     tried = true;
-    attr_ok = set_smem_attr<Exact6, 128>() && set_smem_attr<Split2, 128>();
+    attr_ok = set_smem_attr<Exact6, 128>() && set_smem_attr<Exact6c, 128>() && set_smem_attr<Split2, 128>();
     if (!attr_ok) cudaGetLastError();
   }
   return attr_ok;
@@ -959,7 +959,10 @@ static void oz_prepare_spin(cphf_ctx* c, OzState& z, int s) {
   o.ready = true;
 }
 
-void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, double alpha, double* out) {
+template <class PC>
+static void oz_k_terms_t(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, double alpha,
+                         double* out) {
+  constexpr bool corr = PC::S == 4;  // correction precision (profiled as its own classes)
   const int64_t nao = c->nao, naux = c->naux, no = c->spin[s].nocc;
   const int64_t N = no * nb;
   if (N <= 0 || nao <= 0) return;
@@ -973,7 +976,7 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
   z.braw.ensure((size_t)S * N * ldk * 2, c->counter());
   z.ebraw.ensure((size_t)N * 4, c->counter());
   {
-    ProfScope ps_slice(c, PROF_SLICE, 0.0, 16.0 * N * nao + 12.0 * N * ldk + 12.0 * nao * nb * ldj);
+    ProfScope ps_slice(c, PROF_SLICE_EXACT, 0.0, 16.0 * N * nao + 12.0 * N * ldk + 12.0 * nao * nb * ldj);
     slice_rows_kernel<Exact6, double><<<grid_warps(N, c->num_sms), 256, 0, c->stream>>>(
         bra, N, nao, 0, nao, 0, 1, z.braw.as<__nv_bfloat16>(), ldk, N * ldk, z.ebraw.as<int>());
     z.brat.ensure((size_t)S * nao * nb * ldj * 2, c->counter());
@@ -983,8 +986,10 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
     count_launch(2);
   }
 
-  // chunk of aux functions: T staging (FP32 pair, 8 B) + slices (12 B) per element within ~8 GiB
-  int64_t np = std::max<int64_t>(1, (int64_t(8) << 30) / std::max<int64_t>(20 * N * ldk, 1));
+  // chunk of aux functions: T staging (FP32 pair, 8 B) + slices (12 B) per element within the
+  // context's chunk budget (8 GiB when there is room)
+  const int64_t budget = c->lowp ? c->lowp->budget : (int64_t(8) << 30);
+  int64_t np = std::max<int64_t>(1, budget / std::max<int64_t>(20 * N * ldk, 1));
   if (c->cfg.aux_chunk > 0) np = c->cfg.aux_chunk;
   np = std::min<int64_t>(std::min<int64_t>(np, naux), 65535);
   z.T.ensure((size_t)np * N * ldk * 8, c->counter());
@@ -1017,12 +1022,12 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
       a.e_row = z.ebrat.as<int>();
       a.e_col = os.eO.as<int>();
       a.m_div = nao; a.s_m1 = 1; a.s_m2 = ldk * no; a.s_n = ldk; a.s_p = N * ldk;
-      ProfScope ps(c, PROF_TC_OZAKI, 2.0 * nao * nb * no * no * npc, 0.0);
+      ProfScope ps(c, (corr ? PROF_OZC_TGEN : PROF_OZ_TGEN), 2.0 * nao * nb * no * no * npc, 0.0);
       a.np = (int)npc;
-      launch_batched<Exact6>(c, mBt, mO, a);
+      launch_batched<PC>(c, mBt, mO, a);
     }
     {
-      ProfScope ps_slice(c, PROF_SLICE, 0.0, (double)rows * (16.0 * nao + 12.0 * ldk));
+      ProfScope ps_slice(c, PROF_SLICE_EXACT, 0.0, (double)rows * (16.0 * nao + 12.0 * ldk));
       CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
       colmax_rows_kernel<float2><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
                                                                                z.mxc.as<unsigned long long>());
@@ -1046,8 +1051,8 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
       a.rowscale = z.rowscale.as<double>();
       a.colscale = z.colscale.as<double>();
       a.ld_out = nao;
-      ProfScope ps(c, PROF_TC_OZAKI, 2.0 * nao * N * nao * npc, 2.0 * S * nao * npc * (nao + N));
-      launch_split<Exact6, 128>(c, z, mCd, mT, a);
+      ProfScope ps(c, (corr ? PROF_OZC_KTERM : PROF_TC_OZAKI), 2.0 * nao * N * nao * npc, 2.0 * S * nao * npc * (nao + N));
+      launch_split<PC, 128>(c, z, mCd, mT, a);
     }
     {
       // W-gen: W[Pl][(i,a)][j] (FP32 pair), rows m = j + no a, columns i, K = nu
@@ -1060,12 +1065,12 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
       a.e_row = z.ebraw.as<int>();
       a.e_col = os.eZ.as<int>();
       a.m_div = no; a.s_m1 = 1; a.s_m2 = ldj * no; a.s_n = ldj; a.s_p = N * ldj;
-      ProfScope ps(c, PROF_TC_OZAKI, 2.0 * N * no * nao * npc, 0.0);
+      ProfScope ps(c, (corr ? PROF_OZC_WGEN : PROF_OZ_WGEN), 2.0 * N * no * nao * npc, 0.0);
       a.np = (int)npc;
-      launch_batched<Exact6>(c, mBw, mZ, a);
+      launch_batched<PC>(c, mBw, mZ, a);
     }
     {
-      ProfScope ps_slice(c, PROF_SLICE, 0.0, (double)rows * (16.0 * no + 12.0 * ldj));
+      ProfScope ps_slice(c, PROF_SLICE_EXACT, 0.0, (double)rows * (16.0 * no + 12.0 * ldj));
       CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
       colmax_rows_kernel<float2><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.W.as<float2>(), rows, N, ldj, no,
                                                                                z.mxc.as<unsigned long long>());
@@ -1089,14 +1094,20 @@ void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, d
       a.rowscale = os.sZt.as<double>();
       a.colscale = z.colscale.as<double>();
       a.ld_out = nao;
-      ProfScope ps(c, PROF_TC_OZAKI, 2.0 * nao * N * no * npc, 2.0 * S * no * npc * (nao + N));
-      launch_split<Exact6, 128>(c, z, mZt, mW, a);
+      ProfScope ps(c, (corr ? PROF_OZC_TERM2 : PROF_OZ_TERM2), 2.0 * nao * N * no * npc, 2.0 * S * no * npc * (nao + N));
+      launch_split<PC, 128>(c, z, mZt, mW, a);
     }
   }
   int flag = 0;
   CPHF_CUDA(cudaMemcpyAsync(&flag, z.err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CPHF_CUDA(cudaStreamSynchronize(c->stream));
   if (flag) throw Error(CPHF_ERR_TIMEOUT, "tensor-core FP64 K-term kernel: a bounded pipeline wait expired");
+}
+
+void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, double alpha, double* out,
+                bool correction) {
+  if (correction) oz_k_terms_t<Exact6c>(c, z, s, bra, nb, alpha, out);
+  else oz_k_terms_t<Exact6>(c, z, s, bra, nb, alpha, out);
 }
 
 // ---- split-FP16 operator of the inner solves ----------------------------------------------

@@ -282,6 +282,51 @@ def xc_golden(dims, tag, seed):
     np.savez(HERE / f"{tag}_seed{seed}.npz", **out)
 
 
+def rhs_golden(tag, seed, nspin):
+    """compute_dimensionless_cphf_rhs of pyhessref's RHessSCF / UHessSCF with stub derivative
+    providers returning seeded synthetic skeleton derivatives (core and overlap AO matrices per
+    atom, the electron-interaction bra)."""
+    dims = dict(nao=22, naux=60, nocc=(5,) if nspin == 1 else (5, 4), natm=3, decay=6.0)
+    s = synth.make_system(dims, seed=seed)
+    nao, natm = s.nao, s.natm
+    rng = np.random.default_rng(seed + 500)
+    sym = lambda a: a + np.swapaxes(a, -1, -2)  # noqa: E731
+    f1core = 0.1 * rng.standard_normal((natm, 3, nao, nao))
+    s1ao = 0.1 * sym(rng.standard_normal((natm, 3, nao, nao)))
+    f1el = [0.1 * rng.standard_normal((natm, 3, nao, s.nocc[t])) for t in range(nspin)]
+    mol = _FakeMol(nao, natm)
+
+    class Gen:
+        def __init__(self, arr):
+            self.arr = arr
+
+        def generator_deriv1(self):
+            return lambda A: self.arr[A]
+
+    class El:
+        def get_deriv1_bra(self, mo_coeff, mo_occ):
+            return f1el[0] if nspin == 1 else [f1el[0], f1el[1]]
+
+    out = dict(f1ao_core=np.asfortranarray(np.transpose(f1core, (2, 3, 1, 0))),
+               s1ao=np.asfortranarray(np.transpose(s1ao, (2, 3, 1, 0))), natm=natm, nspin=nspin)
+    if nspin == 1:
+        from pyhessref.hess_scf_restricted import RHessSCF
+        drv = RHessSCF(mol, s.mo_coeff[0], s.mo_occ[0], s.mo_energy[0], Gen(s1ao), [Gen(f1core)], [El()])
+        res = drv.compute_dimensionless_cphf_rhs()
+        res = {k: [v] for k, v in res.items()}
+    else:
+        from pyhessref.hess_scf_unrestricted import UHessSCF
+        drv = UHessSCF(mol, np.stack(s.mo_coeff), np.stack(s.mo_occ), np.stack(s.mo_energy), Gen(s1ao),
+                       [Gen(f1core)], [El()])
+        res = drv.compute_dimensionless_cphf_rhs()
+    for t in range(nspin):
+        out.update({f"mo_coeff{t}": s.mo_coeff[t], f"mo_occ{t}": s.mo_occ[t], f"mo_energy{t}": s.mo_energy[t],
+                    f"f1bra_el{t}": np.asfortranarray(np.transpose(f1el[t], (2, 3, 1, 0))),
+                    f"rhs{t}": _from_py(res["rhs"][t]), f"f1mo{t}": _from_py(res["f1mo"][t]),
+                    f"s1mo{t}": _from_py(res["s1mo"][t])})
+    np.savez(HERE / f"{tag}_seed{seed}.npz", **out)
+
+
 def main():
     if REF is None or not (REF / "pyhessref").is_dir():
         raise SystemExit("set CPHF_REFERENCE to the reference project's root (the directory holding pyhessref/)")
@@ -292,6 +337,8 @@ def main():
     uhf_golden(dict(nao=20, naux=70, nocc=(5, 4), natm=3, decay=6.0), "uhf_nao20", seed=2)
     xc_golden(XC_RKS, "xc_rks_nao30", seed=3)
     xc_golden(XC_UKS, "xc_uks_nao28", seed=4)
+    rhs_golden("rhs_rhf_nao22", seed=5, nspin=1)
+    rhs_golden("rhs_uhf_nao22", seed=6, nspin=2)
     print("golden vectors written to", HERE)
 
 

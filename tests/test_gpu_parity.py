@@ -276,7 +276,8 @@ def test_emulated_fp64_residual(dims, mode):
     res_emul = cmx.last_stats["residual_max"]
     assert cmx.last_stats["residual_mode"] == mode
     if mode == 2:
-        classes = ["kterm_tcgen05_bf16x6_exact"]
+        classes = ["kterm_tcgen05_bf16x6_exact", "tgen_tcgen05_bf16x6_exact", "wgen_tcgen05_bf16x6_exact",
+                   "term2_tcgen05_bf16x6_exact"]
         if s.grid is not None:
             classes.append("xc_tcgen05_bf16x6_exact")
         assert_tensor_core_classes(cmx, classes)
@@ -302,11 +303,16 @@ def test_mixed_precision_solve(dims, dfloat):
     # every correction's residual is recomputed with the FP64-accurate operator (the solve's own
     # final check, verify_residual = 2); convergence is decided on that recomputed residual
     assert st["fp64_matvec_columns"] == st["refine_steps"] * nset
-    assert st["residual_mode"] == dfloat
+    # exact slices: the first correction's residual recomputed in full, later corrections
+    # subtracted with the exact-slice operator in correction precision (residual mode 4)
+    assert st["residual_mode"] == (4 if dfloat == 2 and st["refine_steps"] > 1 else dfloat)
     if dfloat == 2:
-        assert_tensor_core_classes(cmx, ["kterm_tcgen05_f16x3", "kterm_tcgen05_bf16x6_exact"])
-    res64, _ = _max_col_residual(c64, s, xmx)
+        assert_tensor_core_classes(cmx, ["kterm_tcgen05_f16x3", "kterm_tcgen05_bf16x6_exact",
+                                         "kterm_tcgen05_bf16x4c_exact"])
+    res64, xmax = _max_col_residual(c64, s, xmx)
     assert res64 < 1e-8
+    # the solve's own final residual agrees with the native FP64 residual of its answer
+    assert abs(st["residual_max"] - res64) < 1e-9 * max(1.0, xmax), (st["residual_max"], res64)
     if s.nspin == 1:
         x64, xmx = [x64], [xmx]
     for a, b in zip(xmx, x64):
@@ -458,11 +464,39 @@ def test_fp64_solve_with_bad_learned_guess():
     """On an FP64 context the network only supplies x0; the Krylov iteration and its stopping test
     are the reference's, so a bad guess still converges to the plain solution."""
     s = synth.make_system(MEDIUM, seed=32)
-    base = make_ctx(s, cphf_tol=1e-10)
+    # lindep below tol^2, so that the trial-norm stopping test (max(lindep, tol^2)) is tol's
+    base = make_ctx(s, cphf_tol=1e-11, cphf_lindep=1e-24)
     x_ref = base.solve_dimless_cphf(s.rhs[0])
-    bad = make_ctx(s, cphf_tol=1e-10, use_learned_guess=1)
+    bad = make_ctx(s, cphf_tol=1e-11, cphf_lindep=1e-24, use_learned_guess=1)
     bad.set_mlp_weights(_bad_weights())
     x = bad.solve_dimless_cphf(s.rhs[0])
     assert np.abs(x[s.nocc[0]:] - x_ref[s.nocc[0]:]).max() < 1e-8
     res64, _ = _max_col_residual(base, s, x)
     assert res64 < 1e-8
+
+
+@pytest.mark.parametrize("name", ["rhs_rhf_nao22_seed5.npz", "rhs_uhf_nao22_seed6.npz"])
+def test_compute_dimless_cphf_rhs_golden(name):
+    """The GPU right-hand-side assembly against pyhessref's compute_dimensionless_cphf_rhs."""
+    g = load_golden(name)
+    nspin = int(g["nspin"])
+    arg = (lambda v: v[0]) if nspin == 1 else (lambda v: v)
+    ctx = Context()
+    ctx.set_nao(g["mo_coeff0"].shape[0])
+    ctx.make_response_preparation(arg([g[f"mo_coeff{t}"] for t in range(nspin)]),
+                                  arg([g[f"mo_occ{t}"] for t in range(nspin)]),
+                                  arg([g[f"mo_energy{t}"] for t in range(nspin)]))
+    rhs, f1, s1 = ctx.compute_dimless_cphf_rhs(g["f1ao_core"], arg([g[f"f1bra_el{t}"] for t in range(nspin)]),
+                                               g["s1ao"])
+    if nspin == 1:
+        rhs, f1, s1 = [rhs], [f1], [s1]
+    for t in range(nspin):
+        assert rel_err(rhs[t], g[f"rhs{t}"]) < 1e-12
+        assert rel_err(f1[t], g[f"f1mo{t}"]) < 1e-12
+        assert rel_err(s1[t], g[f"s1mo{t}"]) < 1e-12
+    # without the electron-interaction part (f1bra_el = NULL)
+    rhs0, f10, s10 = ctx.compute_dimless_cphf_rhs(g["f1ao_core"], None, g["s1ao"])
+    r_ref, f_ref, s_ref = cphf.compute_dimless_cphf_rhs(g["mo_coeff0"], g["mo_occ0"], g["mo_energy0"], g["f1ao_core"],
+                                                        None, g["s1ao"])
+    assert rel_err(rhs0 if nspin == 1 else rhs0[0], r_ref) < 1e-12
+    assert rel_err(f10 if nspin == 1 else f10[0], f_ref) < 1e-12

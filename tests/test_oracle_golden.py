@@ -180,3 +180,17 @@ def test_j2c_eigenvalue_fallback_and_solve():
     j3c = rng.standard_normal((50, 30))
     cd = decompose.solve_by_j2c_right(j3c, U)
     assert np.allclose(cd @ U, j3c, atol=1e-12)
+
+
+# ---------------------------------------------------------------- CPHF right-hand side
+@pytest.mark.parametrize("name", ["rhs_rhf_nao22_seed5.npz", "rhs_uhf_nao22_seed6.npz"])
+def test_compute_dimless_cphf_rhs_matches_reference(name):
+    """oracle/cphf.py:compute_dimless_cphf_rhs against pyhessref's RHessSCF / UHessSCF
+    compute_dimensionless_cphf_rhs (rscf.rs:104-182, uscf.rs:78-173) on the same derivatives."""
+    g = load_golden(name)
+    for t in range(int(g["nspin"])):
+        rhs, f1, s1 = cphf.compute_dimless_cphf_rhs(g[f"mo_coeff{t}"], g[f"mo_occ{t}"], g[f"mo_energy{t}"],
+                                                    g["f1ao_core"], g[f"f1bra_el{t}"], g["s1ao"])
+        assert rel_err(rhs, g[f"rhs{t}"]) < 1e-13
+        assert rel_err(f1, g[f"f1mo{t}"]) < 1e-13
+        assert rel_err(s1, g[f"s1mo{t}"]) < 1e-13
