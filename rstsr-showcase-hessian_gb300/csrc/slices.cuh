@@ -73,10 +73,12 @@ __device__ __forceinline__ long long fix_round(float x, int k, bool& bad) {
 
 // F = round(v 2^36), |F| <= 2^36, into the six digits q_t = round(R_t / 2^(30 - 6t)) of the
 // running remainder, written as BF16 slices q_t 2^(-6(t+1)) (plane stride `plane`).
+// NS < 6 writes only the leading NS digits (the planes a correction-precision product reads).
+template <int NS = 6>
 __device__ __forceinline__ void digits6(long long F, bool bad, __nv_bfloat16* dst, int64_t plane) {
   long long R = F;
 #pragma unroll
-  for (int t = 0; t < Exact6::S; ++t) {
+  for (int t = 0; t < NS; ++t) {
     const int s = 30 - 6 * t;
     const long long q = s > 0 ? ((R + (1ll << (s - 1))) >> s) : R;
     R -= q << s;
@@ -90,10 +92,11 @@ __device__ __forceinline__ void slice6(double x, int e, __nv_bfloat16* dst, int6
   const long long F = fix_round(x, 36 - e, bad);
   digits6(F, bad, dst, plane);
 }
+template <int NS = 6>
 __device__ __forceinline__ void slice6(float2 x, int e, __nv_bfloat16* dst, int64_t plane) {
   bool bad = false;
   const long long F = fix_round(x.x, 36 - e, bad) + fix_round(x.y, 36 - e, bad);
-  digits6(F, bad, dst, plane);
+  digits6<NS>(F, bad, dst, plane);
 }
 
 // store one element's planes: exact BF16 slices, or split FP16 hi/lo of x 2^(14 - e)
@@ -106,6 +109,7 @@ struct Put<Exact6> {
 };
 template <>
 struct Put<Split2> {
+  __device__ static void put(double x, int e, __half* dst, int64_t plane) { put((float)x, e, dst, plane); }
   __device__ static void put(float x, int e, __half* dst, int64_t plane) {
     const float v = ldexpf(x, Split2::EOFF - e);
     const __half h = __float2half_rn(v);

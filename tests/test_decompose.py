@@ -66,10 +66,12 @@ def test_j2c_small_diagonal_triggers_fallback():
                                        ("rhf_nao600", 0)])
 def test_set_j3c_builds_cderi(dims, seed):
     """j3c = B U^T from a synthetic B and an SPD metric: the GPU recovers B = j3c U^-1 (1e-12
-    relative to the oracle's triangular solve) and the plugin built from it answers like the
-    one built from B.  The second case is the 180-RHS workload's size (nao 600, naux 2000)."""
+    relative to the oracle's triangular solve for a metric of condition number 1e3; two
+    triangular solves in different operation orders differ by ~cond x 1e-16) and the plugin built
+    from it answers like the one built from B.  The second case is the 180-RHS workload's size
+    (nao 600, naux 2000)."""
     s = synth.make_system(dims, seed=seed)
-    j2c = decompose.synthetic_metric(s.naux, seed=seed + 1, cond=1e5)
+    j2c = decompose.synthetic_metric(s.naux, seed=seed + 1, cond=1e3)
     U_ref, _ = decompose.decomp_j2c_cd(j2c, 1e-14)
     j3c = np.asfortranarray(s.cderi @ U_ref)
     cd_ref = decompose.solve_by_j2c_right(j3c, U_ref)
@@ -84,3 +86,17 @@ def test_set_j3c_builds_cderi(dims, seed):
         bra = np.random.default_rng(9).standard_normal((s.nao, s.nocc[0], 3))
         ref = rijk.rhf_response_bra(cd_ref, s.mo_coeff[0], s.mo_occ[0], bra, s.scale_j, s.scale_k)
         assert rel_err(ctx.get_response_bra(bra), ref) < 1e-12
+
+
+def test_set_j3c_ill_conditioned_metric():
+    """Condition number 1e6: the GPU cderi and the oracle's agree to the triangular solve's
+    forward-error scale (cond x 1e-16, with a factor 10 of margin)."""
+    s = synth.make_system(dict(nao=36, naux=200, nocc=(5,), natm=3, decay=8.0), seed=11)
+    cond = 1e6
+    j2c = decompose.synthetic_metric(s.naux, seed=12, cond=cond)
+    U_ref, _ = decompose.decomp_j2c_cd(j2c, 1e-14)
+    j3c = np.asfortranarray(s.cderi @ U_ref)
+    cd_ref = decompose.solve_by_j2c_right(j3c, U_ref)
+    ctx = Context()
+    ctx.set_j3c(j3c, j2c, s.scale_j, s.scale_k)
+    assert rel_err(ctx.get_cderi(), cd_ref) < 10 * cond * 1e-16

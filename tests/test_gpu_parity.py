@@ -446,15 +446,16 @@ def _bad_weights():
     return omlp.pack(d).astype(np.float32)
 
 
-@pytest.mark.parametrize("mode", [1, 2])
-def test_mixed_solve_with_bad_learned_preconditioner(mode):
+@pytest.mark.parametrize("dims,mode", [(MEDIUM, 1), (MEDIUM, 2), (MEDIUM_U, 1), (MEDIUM_U, 2)])
+def test_mixed_solve_with_bad_learned_preconditioner(dims, mode):
     """A deliberately bad network costs iterations, never accuracy: the mixed solve's outer
-    FP64-accurate residual still decides convergence to ||b - (I+A)x|| < 1e-8."""
-    s = synth.make_system(MEDIUM, seed=31)
+    FP64-accurate residual still decides convergence to ||b - (I+A)x|| < 1e-8 (one- and
+    two-spin solves; uscf.rs:278-341 goes through the same x0 hook)."""
+    s = synth.make_system(dims, seed=31)
     c64 = make_ctx(s)
     cmx = make_ctx(s, precision="mixed", use_learned_guess=mode)
     cmx.set_mlp_weights(_bad_weights())
-    x = cmx.solve_dimless_cphf(s.rhs[0])
+    x = cmx.solve_dimless_cphf(s.rhs[0] if s.nspin == 1 else s.rhs)
     assert cmx.last_stats["residual_max"] < 1e-8
     res64, _ = _max_col_residual(c64, s, x)
     assert res64 < 1e-8
