@@ -30,7 +30,6 @@ struct OzState {
   OzSpin spin[2];
   // per-call scratch: bra slices (both K orders), T / Wt staging (FP32 pairs) and slices
   DevBuf braw, ebraw, brat, ebrat, T, B, W, Ws, braS;
-  DevBuf brat16, ebrat16, tmax;  // split-FP16 bra rows and T column maxima (exact T-gen scales)
   DevBuf colscale, e_col, mxc, err, tune_out;
   int64_t ldk = 0;
   bool ready = false;

@@ -108,8 +108,11 @@ struct Put<Exact6> {
   __device__ static void put(T x, int e, __nv_bfloat16* dst, int64_t plane) { slice6(x, e, dst, plane); }
 };
 template <>
+struct Put<Exact6c> {  // only the four planes a correction-precision product reads
+  __device__ static void put(float2 x, int e, __nv_bfloat16* dst, int64_t plane) { slice6<4>(x, e, dst, plane); }
+};
+template <>
 struct Put<Split2> {
-  __device__ static void put(double x, int e, __half* dst, int64_t plane) { put((float)x, e, dst, plane); }
   __device__ static void put(float x, int e, __half* dst, int64_t plane) {
     const float v = ldexpf(x, Split2::EOFF - e);
     const __half h = __float2half_rn(v);

@@ -111,9 +111,6 @@ struct OzArgs {
   const int* e_row;
   const int* e_col;
   int64_t m_div, s_m1, s_m2, s_n, s_p;
-  unsigned* colmax;         // EPI_COLMAX output
-  const int* e_t;           // EPI_SLICE column exponents
-  int64_t plane;            // EPI_SLICE plane stride (elements)
   int* err;
 };
 
@@ -358,11 +355,7 @@ __device__ __forceinline__ float pow2f(int e) {
 }
 
 // EPI: store the scaled values (T / W staging) or FP16 hi / lo planes of them times *tscale
-// EPI_COLMAX (split FP16): no stores; max |value| per output column n_T = n + N (row / m_div)
-// over the CTA's rows and aux functions, atomically into colmax (float bits).
-// EPI_SLICE (exact slices): the value sliced straight into its BF16 planes (the first PR::S of
-// six) with the exponent e_t[n_T] of its column n_T = n + N (row / m_div), plane stride `plane`.
-enum { EPI_STORE = 0, EPI_SPLIT16 = 2, EPI_COLMAX = 3, EPI_SLICE = 4 };
+enum { EPI_STORE = 0, EPI_SPLIT16 = 2 };
 
 template <class PR, int BN, int EPI = EPI_STORE>
 __global__ void __launch_bounds__(320, PR::NACC == 4 ? 1 : 2)
@@ -487,22 +480,6 @@ __global__ void __launch_bounds__(320, PR::NACC == 4 ? 1 : 2)
         base = args.m_div > 0 ? (row % args.m_div) * args.s_m1 + (row / args.m_div) * args.s_m2 : row * args.s_m1;
       }
       const int ncol = n0 + c * 32 + lane;  // the column whose exponent this lane fetches
-      // EPI_COLMAX / EPI_SLICE: the row's block index a = row / m_div selects the output column
-      // n_T = n + N a; EPI_SLICE keeps this thread's 32 column exponents for every aux function
-      const int64_t arow = (row_ok && args.m_div > 0) ? row / args.m_div : 0;
-      float cmax[EPI == EPI_COLMAX ? 32 : 1];
-      int et[EPI == EPI_SLICE ? 32 : 1];
-      if constexpr (EPI == EPI_COLMAX) {
-#pragma unroll
-        for (int j = 0; j < 32; ++j) cmax[j] = 0.f;
-      }
-      if constexpr (EPI == EPI_SLICE) {
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int n = n0 + c * 32 + j;
-          et[j] = (row_ok && n < args.N) ? args.e_t[n + (int64_t)args.N * arow] : 0;
-        }
-      }
       for (int p = 0; p < nP; ++p) {
         const int b = p & 1;
         // warp-uniform decision: tcgen05.ld is a whole-warp instruction
@@ -525,12 +502,7 @@ __global__ void __launch_bounds__(320, PR::NACC == 4 ? 1 : 2)
             if (row_ok && n < args.N) {
               float hi, lo;
               combine4(v0[j], v1[j], v2[j], v3[j], hi, lo);
-              if constexpr (EPI == EPI_SLICE) {
-                slice6<PR::S>(make_float2(hi * f, lo * f), et[j],
-                              reinterpret_cast<__nv_bfloat16*>(args.out) + pbase + n * args.s_n, args.plane);
-              } else {
-                reinterpret_cast<float2*>(args.out)[pbase + n * args.s_n] = make_float2(hi * f, lo * f);
-              }
+              reinterpret_cast<float2*>(args.out)[pbase + n * args.s_n] = make_float2(hi * f, lo * f);
             }
           }
         } else {
@@ -544,8 +516,6 @@ __global__ void __launch_bounds__(320, PR::NACC == 4 ? 1 : 2)
             if (row_ok && n < args.N) {
               if constexpr (EPI == EPI_STORE) {
                 reinterpret_cast<float*>(args.out)[pbase + n * args.s_n] = v[j] * f;
-              } else if constexpr (EPI == EPI_COLMAX) {
-                cmax[j] = fmaxf(cmax[j], fabsf(v[j] * f));
               } else {
                 const float x = (v[j] * f) * ts;
                 const __half h = __float2half_rn(x);
@@ -559,25 +529,6 @@ __global__ void __launch_bounds__(320, PR::NACC == 4 ? 1 : 2)
         fence_before_sync();
         __syncwarp();
         if (lane == 0) mbar_arrive(acce0 + 8 * b);
-      }
-      if constexpr (EPI == EPI_COLMAX) {
-        // column maxima over the warp's 32 rows: one atomic per column when the rows share a
-        // block index, else one per row
-        const bool ok = row_ok;
-        const int64_t a0 = __shfl_sync(0xffffffffu, arow, 0);
-        const bool uniform = __all_sync(0xffffffffu, !ok || arow == a0) && __any_sync(0xffffffffu, ok);
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int n = n0 + c * 32 + j;
-          if (n >= args.N) continue;
-          float m = ok ? cmax[j] : 0.f;
-          if (uniform) {
-            for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-            if (lane == 0) atomicMax(args.colmax + n + (int64_t)args.N * a0, __float_as_uint(m));
-          } else if (ok) {
-            atomicMax(args.colmax + n + (int64_t)args.N * arow, __float_as_uint(m));
-          }
-        }
       }
     }
   }
@@ -627,21 +578,6 @@ __global__ void exp_scale_kernel(const unsigned long long* __restrict__ mx, int6
   const int e = key_exp(mx[i], is_float);
   e_out[i] = e;
   scale[i] = mult * ldexp(1.0, e - eoff);
-}
-
-// T's column exponents from its column maxima estimated in split FP16 (float bits; ~1e-6
-// relative): e with max (1 + 2^-10) < 2^e, scale = mult 2^e.  The margin covers the estimate's
-// error; a true maximum up to 2^-10 above the estimate would still only reach 2^36 (1 + 2^-10)
-// in the fixed-point form, which the leading digit (|q_0| <= 64) absorbs.
-__global__ void tmax_scale_kernel(const unsigned* __restrict__ mx, int64_t n, double mult, int* __restrict__ e_out,
-                                  double* __restrict__ scale) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float m = __uint_as_float(mx[i]) * (1.0f + 1.0f / 1024.0f);
-  int e = 0;
-  if (m > 0.f && isfinite(m)) frexpf(m, &e);
-  e_out[i] = e;
-  scale[i] = mult * ldexp(1.0, e);
 }
 
 // cderi slices [t][P][mu][ldk] of B_P[mu, nu] 2^-e_mu (B_P symmetric: read Bd[nu + nao mu + nao^2 P])
@@ -797,22 +733,14 @@ bool set_short_smem_attr() {
 
 template <class PR, int BN>
 bool set_smem_attr() {
-  bool ok = cudaFuncSetAttribute(tc_slice_kernel<PR, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 Cfg<PR, BN>::SMEM_BYTES) == cudaSuccess &&
-            set_short_smem_attr<PR, BN>() &&
-            cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 Batched<PR>::SMEM_BYTES) == cudaSuccess;
-  if constexpr (PR::NACC == 4) {
-    ok = ok && cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64, EPI_SLICE>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, Batched<PR>::SMEM_BYTES) == cudaSuccess;
-  } else {
-    ok = ok &&
-         cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64, EPI_SPLIT16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(tc_slice_kernel<PR, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              Cfg<PR, BN>::SMEM_BYTES) == cudaSuccess &&
+         set_short_smem_attr<PR, BN>() &&
+         cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               Batched<PR>::SMEM_BYTES) == cudaSuccess &&
-         cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64, EPI_COLMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              Batched<PR>::SMEM_BYTES) == cudaSuccess;
-  }
-  return ok;
+         (PR::NACC == 4 ||
+          cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64, EPI_SPLIT16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               Batched<PR>::SMEM_BYTES) == cudaSuccess);
 }
 
 // ---- launch-shape autotuner ---------------------------------------------------------------
@@ -1031,8 +959,6 @@ static void oz_prepare_spin(cphf_ctx* c, OzState& z, int s) {
   o.ready = true;
 }
 
-static void lp_prepare_spin(cphf_ctx* c, OzState& z, int s);
-
 template <class PC>
 static void oz_k_terms_t(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, double alpha,
                          double* out) {
@@ -1060,29 +986,14 @@ static void oz_k_terms_t(cphf_ctx* c, OzState& z, int s, const double* bra, int6
     count_launch(2);
   }
 
-  // split-FP16 planes of the same bra (rows (nu, a) over j) and of O: T's column maxima come
-  // from a three-product pass that stores nothing, so that the exact T-gen can slice T in its
-  // epilogue (no FP32 T staging, no max or slicing pass over it)
-  OzState& lpz = c->lowp->lp;
-  if (!lpz.spin[s].ready) lp_prepare_spin(c, lpz, s);
-  const OzSpin& ls = lpz.spin[s];
-  z.brat16.ensure((size_t)2 * nao * nb * ldj * 2, c->counter());
-  z.ebrat16.ensure((size_t)nao * nb * 4, c->counter());
-  {
-    ProfScope ps_slice(c, PROF_SLICE_EXACT, 0.0, 8.0 * N * nao + 4.0 * nao * nb * ldj);
-    slice_rows_kernel<Split2, double><<<grid_warps(nao * nb, c->num_sms), 256, 0, c->stream>>>(
-        bra, nao * nb, no, nao, 1, nao * no, nao, z.brat16.as<__half>(), ldj, nao * nb * ldj, z.ebrat16.as<int>());
-    count_launch();
-  }
-
-  // chunk of aux functions: T slices (2 B per plane) and W staging (FP32 pair) + slices per
-  // element within the context's chunk budget (8 GiB when there is room)
+  // chunk of aux functions: T staging (FP32 pair, 8 B) + slices (12 B) per element within the
+  // context's chunk budget (8 GiB when there is room)
   const int64_t budget = c->lowp ? c->lowp->budget : (int64_t(8) << 30);
-  int64_t np = std::max<int64_t>(1, budget / std::max<int64_t>(2 * PC::S * N * ldk + 20 * N * ldj, 1));
+  int64_t np = std::max<int64_t>(1, budget / std::max<int64_t>(20 * N * ldk, 1));
   if (c->cfg.aux_chunk > 0) np = c->cfg.aux_chunk;
   np = std::min<int64_t>(std::min<int64_t>(np, naux), 65535);
+  z.T.ensure((size_t)np * N * ldk * 8, c->counter());
   z.B.ensure((size_t)S * np * N * ldk * 2, c->counter());
-  z.tmax.ensure((size_t)N * 4, c->counter());
   z.W.ensure((size_t)np * N * ldj * 8, c->counter());
   z.Ws.ensure((size_t)S * np * N * ldj * 2, c->counter());
   z.colscale.ensure((size_t)N * 8, c->counter());
@@ -1091,8 +1002,6 @@ static void oz_k_terms_t(cphf_ctx* c, OzState& z, int s, const double* bra, int6
 
   const CUtensorMap mCd = make_map(z.A.p, nao, nao, S * naux, ldk, BM);            // term 1 A
   const CUtensorMap mBt = make_map(z.brat.p, no, nao * nb, S, ldj, BM);            // T-gen A
-  const CUtensorMap mBt16 = make_map(z.brat16.p, no, nao * nb, 2, ldj, BM, false);  // T max pass A
-  const CUtensorMap mO16 = make_map(ls.O.p, no, no, 2 * naux, ldj, 64, false);     // T max pass B
   const CUtensorMap mO = make_map(os.O.p, no, no, S * naux, ldj, 64);               // T-gen B
   const CUtensorMap mBw = make_map(z.braw.p, nao, N, S, ldk, BM);                  // W-gen A
   const CUtensorMap mZ = make_map(os.Z.p, nao, no, S * naux, ldk, 64);             // W-gen B
@@ -1103,42 +1012,30 @@ static void oz_k_terms_t(cphf_ctx* c, OzState& z, int s, const double* bra, int6
     const int64_t npc = std::min<int64_t>(np, naux - P0);
     const int64_t rows = npc * N;
     {
-      // column maxima of T over the chunk (split FP16, three products, nothing stored), then
-      // the exponents and scales of T's columns n = i + nocc a
+      // T-gen: T[Pl][(i,a)][nu] (FP32 pair), rows m = nu + nao a, columns i, K = j
       OzArgs a = base_args(z, (int)(nao * nb), (int)no);
-      a.nkb = nkb_no;
-      a.a_depth = 1;
-      a.b_depth = (int)naux;
-      a.b_off = (int)P0;
-      a.e_row = z.ebrat16.as<int>();
-      a.e_col = ls.eO.as<int>();
-      a.m_div = nao;
-      a.colmax = z.tmax.as<unsigned>();
-      a.np = (int)npc;
-      ProfScope ps(c, PROF_SLICE_EXACT, 2.0 * nao * nb * no * no * npc, 0.0);
-      CPHF_CUDA(cudaMemsetAsync(z.tmax.p, 0, (size_t)N * 4, c->stream));
-      launch_batched<Split2, EPI_COLMAX>(c, mBt16, mO16, a);
-      tmax_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.tmax.as<unsigned>(), N, alpha, z.e_col.as<int>(),
-                                                            z.colscale.as<double>());
-      count_launch();
-    }
-    {
-      // T-gen: T[Pl][(i,a)][nu] straight into its BF16 slice planes (column exponents e_col),
-      // rows m = nu + nao a, columns i, K = j
-      OzArgs a = base_args(z, (int)(nao * nb), (int)no);
-      a.out = z.B.p;
+      a.out = z.T.p;
       a.nkb = nkb_no;
       a.a_depth = 1;
       a.b_depth = (int)naux;
       a.b_off = (int)P0;
       a.e_row = z.ebrat.as<int>();
       a.e_col = os.eO.as<int>();
-      a.e_t = z.e_col.as<int>();
-      a.plane = rows * ldk;
       a.m_div = nao; a.s_m1 = 1; a.s_m2 = ldk * no; a.s_n = ldk; a.s_p = N * ldk;
-      ProfScope ps(c, (corr ? PROF_OZC_TGEN : PROF_OZ_TGEN), 2.0 * nao * nb * no * no * npc, 2.0 * PC::S * rows * ldk);
+      ProfScope ps(c, (corr ? PROF_OZC_TGEN : PROF_OZ_TGEN), 2.0 * nao * nb * no * no * npc, 0.0);
       a.np = (int)npc;
-      launch_batched<PC, EPI_SLICE>(c, mBt, mO, a);
+      launch_batched<PC>(c, mBt, mO, a);
+    }
+    {
+      ProfScope ps_slice(c, PROF_SLICE_EXACT, 0.0, (double)rows * (16.0 * nao + 12.0 * ldk));
+      CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
+      colmax_rows_kernel<float2><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
+                                                                               z.mxc.as<unsigned long long>());
+      exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true, 0,
+                                                           z.e_col.as<int>(), z.colscale.as<double>());
+      slice_staging_kernel<PC, float2><<<grid_for(rows * nao), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
+                                                                     z.e_col.as<int>(), z.B.as<__nv_bfloat16>());
+      count_launch(3);
     }
     {
       // term 1: out[mu, n] += alpha sum_{P, nu} B_P[mu, nu] T_P[nu, n]
@@ -1179,7 +1076,7 @@ static void oz_k_terms_t(cphf_ctx* c, OzState& z, int s, const double* bra, int6
                                                                                z.mxc.as<unsigned long long>());
       exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true, 0,
                                                            z.e_col.as<int>(), z.colscale.as<double>());
-      slice_staging_kernel<Exact6, float2><<<grid_for(rows * no), 256, 0, c->stream>>>(z.W.as<float2>(), rows, N, ldj, no,
+      slice_staging_kernel<PC, float2><<<grid_for(rows * no), 256, 0, c->stream>>>(z.W.as<float2>(), rows, N, ldj, no,
                                                                      z.e_col.as<int>(), z.Ws.as<__nv_bfloat16>());
       count_launch(3);
     }
