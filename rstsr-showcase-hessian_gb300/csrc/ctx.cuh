@@ -231,6 +231,7 @@ struct cphf_ctx {
   bool f64_emulate = false;  // route the FP64 GEMMs through the double-float kernel
   bool oz_kterm = false;     // FP64 K term 1 on the tensor cores (exact BF16 slices)
   bool oz_correction = false;  // ... in correction precision (slices 0-3, 10 products)
+  bool f32_correction = false; // FP64 GEMMs of a correction-precision application run in FP32
   bool oz_xc = false;        // FP64 XC response on the tensor cores (exact BF16 slices)
 
   int64_t* counter() { return &device_bytes; }

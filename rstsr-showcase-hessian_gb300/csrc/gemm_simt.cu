@@ -286,6 +286,7 @@ CPHF_INST(float, double, float, float)
 CPHF_INST(float, float, double, double)
 CPHF_INST(float, double, double, float)
 CPHF_INST(float, double, float, double)
+CPHF_INST(float, double, double, double)
 #undef CPHF_INST
 
 cudaError_t gemm_f64_emulated(const GemmDesc& d, cudaStream_t stream, void* workspace, size_t ws_bytes,

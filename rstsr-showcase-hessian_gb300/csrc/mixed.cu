@@ -349,6 +349,7 @@ AccurateScope::AccurateScope(cphf_ctx* ctx, int mode, bool correction) : c(ctx) 
   c->oz_kterm = mode == 2 && c->has_rijk && tc && oz_supported(c);
   c->oz_xc = mode == 2 && c->has_xc && tc;
   c->oz_correction = correction && c->oz_kterm;
+  c->f32_correction = c->oz_correction;  // the correction's J, C x and C^T r GEMMs to ~1e-7 of it
   // mode 2 without any tensor-core contraction available is the double-float operator
   used = mode == 2 && !(c->oz_kterm || c->oz_xc) ? 1 : mode;
 }
@@ -358,6 +359,7 @@ AccurateScope::~AccurateScope() {
   c->oz_kterm = false;
   c->oz_xc = false;
   c->oz_correction = false;
+  c->f32_correction = false;
 }
 
 bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, double* x, cphf_stats* st,

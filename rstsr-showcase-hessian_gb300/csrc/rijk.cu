@@ -37,6 +37,12 @@ const char* const kProfNames[PROF_NCLASS] = {"gemm_fp64_simt", "gemm_fp32_simt",
 static double gemm_flops(const GemmDesc& d) { return 2.0 * d.M * d.N * d.K * d.batch1 * d.batch2; }
 
 void gemm64(cphf_ctx* c, const GemmDesc& d) {
+  if (c->f32_correction) {
+    // FP64 operands and result, FP32 arithmetic: the GEMMs of an operator applied to a small
+    // correction, whose result is needed only to ~1e-7 of the correction itself
+    gemm32x<double, double, double>(c, d);
+    return;
+  }
   const size_t need = gemm_workspace_bytes(d, 8, c->num_sms);
   if (need) c->ws_gemm.ensure(need, c->counter());
   if (c->f64_emulate) {
@@ -64,6 +70,7 @@ template void gemm32x<double, float, float>(cphf_ctx*, const GemmDesc&);
 template void gemm32x<float, double, double>(cphf_ctx*, const GemmDesc&);
 template void gemm32x<double, double, float>(cphf_ctx*, const GemmDesc&);
 template void gemm32x<double, float, double>(cphf_ctx*, const GemmDesc&);
+template void gemm32x<double, double, double>(cphf_ctx*, const GemmDesc&);
 
 void rijk_prepare(cphf_ctx* c) {
   const int64_t nao = c->nao, naux = c->naux;

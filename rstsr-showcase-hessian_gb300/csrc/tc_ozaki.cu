@@ -111,6 +111,7 @@ struct OzArgs {
   const int* e_row;
   const int* e_col;
   int64_t m_div, s_m1, s_m2, s_n, s_p;
+  unsigned long long* colmax;  // EPI_STOREMAX: column maxima (float bits of |value|)
   int* err;
 };
 
@@ -354,8 +355,11 @@ __device__ __forceinline__ float pow2f(int e) {
   return (e >= -126 && e <= 127) ? __int_as_float((e + 127) << 23) : ldexpf(1.f, e);
 }
 
-// EPI: store the scaled values (T / W staging) or FP16 hi / lo planes of them times *tscale
-enum { EPI_STORE = 0, EPI_SPLIT16 = 2 };
+// EPI: store the scaled values (T / W staging) or FP16 hi / lo planes of them times *tscale.
+// EPI_STOREMAX (exact slices): store as EPI_STORE and reduce max |value| per staging column
+// n_T = n + N (row / m_div) over the CTA's rows and aux functions into colmax (the column
+// scales of the next slicing pass, without a pass over the staging array).
+enum { EPI_STORE = 0, EPI_STOREMAX = 1, EPI_SPLIT16 = 2 };
 
 template <class PR, int BN, int EPI = EPI_STORE>
 __global__ void __launch_bounds__(320, PR::NACC == 4 ? 1 : 2)
@@ -480,6 +484,13 @@ __global__ void __launch_bounds__(320, PR::NACC == 4 ? 1 : 2)
         base = args.m_div > 0 ? (row % args.m_div) * args.s_m1 + (row / args.m_div) * args.s_m2 : row * args.s_m1;
       }
       const int ncol = n0 + c * 32 + lane;  // the column whose exponent this lane fetches
+      // EPI_STOREMAX: the row's block index a = row / m_div selects the staging column n + N a
+      const int64_t arow = (row_ok && args.m_div > 0) ? row / args.m_div : 0;
+      float cmax[EPI == EPI_STOREMAX ? 32 : 1];
+      if constexpr (EPI == EPI_STOREMAX) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) cmax[j] = 0.f;
+      }
       for (int p = 0; p < nP; ++p) {
         const int b = p & 1;
         // warp-uniform decision: tcgen05.ld is a whole-warp instruction
@@ -503,6 +514,7 @@ __global__ void __launch_bounds__(320, PR::NACC == 4 ? 1 : 2)
               float hi, lo;
               combine4(v0[j], v1[j], v2[j], v3[j], hi, lo);
               reinterpret_cast<float2*>(args.out)[pbase + n * args.s_n] = make_float2(hi * f, lo * f);
+              if constexpr (EPI == EPI_STOREMAX) cmax[j] = fmaxf(cmax[j], fabsf(hi * f));
             }
           }
         } else {
@@ -529,6 +541,24 @@ __global__ void __launch_bounds__(320, PR::NACC == 4 ? 1 : 2)
         fence_before_sync();
         __syncwarp();
         if (lane == 0) mbar_arrive(acce0 + 8 * b);
+      }
+      if constexpr (EPI == EPI_STOREMAX) {
+        // column maxima over the warp's 32 rows: one atomic per column when the rows share a
+        // block index, else one per row
+        const int64_t a0 = __shfl_sync(0xffffffffu, arow, 0);
+        const bool uniform = __all_sync(0xffffffffu, !row_ok || arow == a0) && __any_sync(0xffffffffu, row_ok);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int n = n0 + c * 32 + j;
+          if (n >= args.N) continue;
+          float m = row_ok ? cmax[j] : 0.f;
+          if (uniform) {
+            for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if (lane == 0) atomicMax(args.colmax + n + (int64_t)args.N * a0, (unsigned long long)__float_as_uint(m));
+          } else if (row_ok) {
+            atomicMax(args.colmax + n + (int64_t)args.N * arow, (unsigned long long)__float_as_uint(m));
+          }
+        }
       }
     }
   }
@@ -733,14 +763,18 @@ bool set_short_smem_attr() {
 
 template <class PR, int BN>
 bool set_smem_attr() {
-  return cudaFuncSetAttribute(tc_slice_kernel<PR, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              Cfg<PR, BN>::SMEM_BYTES) == cudaSuccess &&
-         set_short_smem_attr<PR, BN>() &&
-         cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              Batched<PR>::SMEM_BYTES) == cudaSuccess &&
-         (PR::NACC == 4 ||
-          cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64, EPI_SPLIT16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               Batched<PR>::SMEM_BYTES) == cudaSuccess);
+  bool ok = cudaFuncSetAttribute(tc_slice_kernel<PR, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 Cfg<PR, BN>::SMEM_BYTES) == cudaSuccess &&
+            set_short_smem_attr<PR, BN>() &&
+            cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 Batched<PR>::SMEM_BYTES) == cudaSuccess;
+  if constexpr (PR::NACC == 4)
+    ok = ok && cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64, EPI_STOREMAX>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, Batched<PR>::SMEM_BYTES) == cudaSuccess;
+  else
+    ok = ok && cudaFuncSetAttribute(tc_slice_batched_kernel<PR, 64, EPI_SPLIT16>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, Batched<PR>::SMEM_BYTES) == cudaSuccess;
+  return ok;
 }
 
 // ---- launch-shape autotuner ---------------------------------------------------------------
@@ -1022,20 +1056,19 @@ static void oz_k_terms_t(cphf_ctx* c, OzState& z, int s, const double* bra, int6
       a.e_row = z.ebrat.as<int>();
       a.e_col = os.eO.as<int>();
       a.m_div = nao; a.s_m1 = 1; a.s_m2 = ldk * no; a.s_n = ldk; a.s_p = N * ldk;
+      a.colmax = z.mxc.as<unsigned long long>();  // T's column maxima, reduced in the epilogue
       ProfScope ps(c, (corr ? PROF_OZC_TGEN : PROF_OZ_TGEN), 2.0 * nao * nb * no * no * npc, 0.0);
       a.np = (int)npc;
-      launch_batched<PC>(c, mBt, mO, a);
+      CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
+      launch_batched<PC, EPI_STOREMAX>(c, mBt, mO, a);
     }
     {
-      ProfScope ps_slice(c, PROF_SLICE_EXACT, 0.0, (double)rows * (16.0 * nao + 12.0 * ldk));
-      CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
-      colmax_rows_kernel<float2><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
-                                                                               z.mxc.as<unsigned long long>());
+      ProfScope ps_slice(c, PROF_SLICE_EXACT, 0.0, (double)rows * (8.0 * nao + 2.0 * PC::S * ldk));
       exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true, 0,
                                                            z.e_col.as<int>(), z.colscale.as<double>());
       slice_staging_kernel<PC, float2><<<grid_for(rows * nao), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
                                                                      z.e_col.as<int>(), z.B.as<__nv_bfloat16>());
-      count_launch(3);
+      count_launch(2);
     }
     {
       // term 1: out[mu, n] += alpha sum_{P, nu} B_P[mu, nu] T_P[nu, n]
