@@ -194,6 +194,20 @@ cphf_status cphf_rijk_get_cderi(cphf_ctx* ctx, double* cderi);
 cphf_status cphf_xc_set_grid(cphf_ctx* ctx, const double* ao, const double* weights,
                              const double* fxc, int64_t ngrids, int32_t nspin,
                              const int64_t* batch_offsets, int64_t nbatch);
+/* The same plugin for every density type of the reference (XCDenType, src/xceff/flags.rs:33-55):
+ *   den_type 0 RHO (LDA, nvar 1), 1 SIGMA (GGA, nvar 4: rho and its gradient), 2 TAU (meta-GGA,
+ *   nvar 5: plus tau);
+ *   ao [ngrids, nao, ncomp]: AO values (component 0) and first derivatives x, y, z (1-3), the
+ *     reference's get_cached_ao(1) tensor; SIGMA / TAU need ncomp >= 4 (only 0-3 are read);
+ *   fxc_eff nspin=1: [ngrids, nvar, nvar]; nspin=2: [ngrids, nvar, 2, nvar, 2] (x, s_in, y, s_out),
+ *     the reference's intmd["cpks_fxc"];
+ *   batch_offsets: as for cphf_xc_set_grid (RHO only; SIGMA / TAU chunk the points themselves).
+ * RHO is cphf_xc_set_grid on component 0.  SIGMA / TAU evaluate rho1's gradient / tau terms
+ * (pure_eval_rho.rs:289-316) and contract_ao_wv_bra's (pure_xcpot.rs:335-351) with dense AO
+ * values on the CUDA cores (FP64; FP32 in the mixed solve's inner operator). */
+cphf_status cphf_xc_set_grid_ex(cphf_ctx* ctx, int32_t den_type, const double* ao, int32_t ncomp,
+                                const double* weights, const double* fxc_eff, int64_t ngrids, int32_t nspin,
+                                const int64_t* batch_offsets, int64_t nbatch);
 /* Declare nao when no RI-JK plugin is used. */
 cphf_status cphf_set_nao(cphf_ctx* ctx, int64_t nao);
 

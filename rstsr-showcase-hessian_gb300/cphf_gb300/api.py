@@ -38,7 +38,7 @@ EXPORTS = [
     "cphf_ctx_profile", "cphf_ctx_profile_report", "cphf_mlp_get_weights", "cphf_mlp_features",
     "cphf_mlp_forward", "cphf_mlp_loss_grad", "cphf_mlp_train", "cphf_rij_noalloc_capacity",
     "cphf_rij_response_bra_noalloc", "cphf_j2c_decompose", "cphf_rijk_set_j3c", "cphf_rijk_get_cderi",
-    "cphf_compute_dimless_cphf_rhs",
+    "cphf_compute_dimless_cphf_rhs", "cphf_xc_set_grid_ex",
 ]
 MLP_NWEIGHTS = 4546
 
@@ -175,6 +175,7 @@ def load_library():
         "cphf_rijk_set_j3c": ([vp, vp, vp, i64, i64, dbl, dbl, dbl, ctypes.POINTER(J2cInfo)], i32),
         "cphf_rijk_get_cderi": ([vp, vp], i32),
         "cphf_compute_dimless_cphf_rhs": ([vp, vp, pp, vp, i64, pp, pp, pp], i32),
+        "cphf_xc_set_grid_ex": ([vp, i32, vp, i32, vp, vp, i64, i32, vp, i64], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -388,6 +389,23 @@ class Context:
             nb = len(offs_arr) - 1
         self._check(self.lib.cphf_xc_set_grid(self.h, k.ptr(ao), k.ptr(weights), k.ptr(fxc), ngrids, nspin,
                                               offs, nb))
+
+    def set_grid_ex(self, den_type, ao, weights, fxc_eff, nspin=1, batch_offsets=None):
+        """XC plugin of any density type: ``den_type`` "rho" / "sigma" / "tau" (or 0 / 1 / 2),
+        ``ao [ngrids, nao, ncomp]`` (value and first derivatives), ``fxc_eff [ngrids, nvar, nvar]``
+        (RKS) or ``[ngrids, nvar, 2, nvar, 2]`` (UKS)."""
+        den = {"rho": 0, "sigma": 1, "tau": 2}.get(den_type, den_type)
+        k = _Keep()
+        ao = np.asarray(ao) if not _is_torch(ao) else ao
+        ngrids, ncomp = ao.shape[0], (ao.shape[2] if len(ao.shape) > 2 else 1)
+        offs, nb = None, 0
+        if batch_offsets is not None:
+            offs_arr = np.ascontiguousarray(batch_offsets, dtype=np.int64)
+            k.refs.append(offs_arr)
+            offs = ctypes.c_void_p(offs_arr.ctypes.data)
+            nb = len(offs_arr) - 1
+        self._check(self.lib.cphf_xc_set_grid_ex(self.h, den, k.ptr(ao), ncomp, k.ptr(weights), k.ptr(fxc_eff),
+                                                 ngrids, nspin, offs, nb))
 
     def make_response_preparation(self, mo_coeff, mo_occ, mo_energy):
         """``make_response_preparation`` plus orbital energies; RHF arrays or UHF two-spin lists."""

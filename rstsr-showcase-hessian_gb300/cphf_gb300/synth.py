@@ -146,6 +146,39 @@ def make_grid(rng, nao, natm, points_range=(8000, 14000), window=80, nspin=1):
     return Grid(ao=ao, weights=weights, fxc=_fortran(fxc), atom_offsets=offsets, window=window)
 
 
+def make_mgga_grid(grid, den, seed=0, nspin=1, coupling=0.1):
+    """Gradient-dependent XC data on an LDA grid: ``ao [ngrids, nao, 4]`` (the grid's values plus
+    three seeded derivative components with the same AO windows) and ``fxc_eff`` of density type
+    ``den`` ("sigma": nvar 4, "tau": nvar 5) -- ``[ngrids, nvar, nvar]`` (RKS) or
+    ``[ngrids, nvar, 2, nvar, 2]`` (UKS), symmetric under ``(x, s_in) <-> (y, s_out)``, with the
+    grid's LDA kernel in the density-density block and seeded couplings of relative size
+    ``coupling`` elsewhere (the shapes of the reference's ``get_cached_ao(1)`` and
+    ``intmd["cpks_fxc"]``)."""
+    rng = np.random.default_rng(seed)
+    ng, nao = grid.ao.shape
+    nvar = {"sigma": 4, "tau": 5}[den]
+    ao = np.zeros((ng, nao, 4), order="F")
+    ao[:, :, 0] = grid.ao
+    mask = grid.ao != 0.0
+    for t in range(1, 4):
+        ao[:, :, t] = np.where(mask, rng.standard_normal((ng, nao)) * np.abs(grid.ao).max(axis=0, keepdims=True), 0.0)
+    if nspin == 1:
+        f00 = np.asarray(grid.fxc).reshape(ng)
+        x = rng.standard_normal((ng, nvar, nvar)) * coupling * np.abs(f00)[:, None, None]
+        fxc = 0.5 * (x + x.transpose(0, 2, 1))
+        fxc[:, 0, 0] = f00
+    else:
+        fl = np.asarray(grid.fxc).reshape(ng, 2, 2)
+        x = rng.standard_normal((ng, nvar * 2, nvar * 2)) * coupling * np.abs(fl).max(axis=(1, 2))[:, None, None]
+        x = 0.5 * (x + x.transpose(0, 2, 1))               # index (x, s) -> x + nvar s
+        for si in range(2):
+            for so in range(2):
+                x[:, nvar * si, nvar * so] = fl[:, si, so]
+        # [g, (x, s_in), (y, s_out)] -> [g, x, s_in, y, s_out]
+        fxc = x.reshape(ng, 2, nvar, 2, nvar).transpose(0, 2, 1, 4, 3)
+    return ao, np.asfortranarray(fxc)
+
+
 class _PowerOperator:
     """Response on the vir-occ block, used only to set the synthetic scale (float32).
 

@@ -429,9 +429,56 @@ cphf_status cphf_xc_set_grid(cphf_ctx* c, const double* ao, const double* weight
     c->xc_plans.clear();  // chunk plans depend on the batches
     c->ngrids = ngrids;
     c->xc_nspin = nspin;
+    c->xc_den = 0;
+    c->xc_nvar = 1;
+    c->phiG.release();
+    c->fxcG.release();
     c->has_xc = true;
     c->prepared = false;
     lowp_release(c);
+  });
+}
+
+cphf_status cphf_xc_set_grid_ex(cphf_ctx* c, int32_t den_type, const double* ao, int32_t ncomp, const double* weights,
+                                const double* fxc_eff, int64_t ngrids, int32_t nspin, const int64_t* batch_offsets,
+                                int64_t nbatch) {
+  if (den_type == 0) {  // RHO: component 0 of ao, fxc_eff [ngrids, 1, 1] / [ngrids, 1, 2, 1, 2]
+    if (!c) return CPHF_ERR_ARG;
+    if (ncomp < 1) {
+      c->last_error = "ncomp must be at least 1";
+      return CPHF_ERR_ARG;
+    }
+    return cphf_xc_set_grid(c, ao, weights, fxc_eff, ngrids, nspin, batch_offsets, nbatch);
+  }
+  return guarded(c, [&] {
+    CPHF_CHECK_ARG(c->nao > 0, "set cderi or nao before the XC grid");
+    CPHF_CHECK_ARG(den_type == 1 || den_type == 2, "den_type must be 0 (RHO), 1 (SIGMA) or 2 (TAU)");
+    CPHF_CHECK_ARG(ncomp >= 4, "SIGMA / TAU need the AO values and their three first derivatives (ncomp >= 4)");
+    CPHF_CHECK_ARG(ngrids >= 0, "ngrids must be non-negative");
+    CPHF_CHECK_ARG(nspin == 1 || nspin == 2, "nspin must be 1 or 2");
+    const int64_t nao = c->nao, nvar = den_type == 1 ? 4 : 5;
+    c->phiG.ensure((size_t)std::max<int64_t>(ngrids * nao * 4, 1) * 8, c->counter());
+    copy_in(c, c->phiG.p, ao, (size_t)ngrids * nao * 4 * 8);  // components 0-3 of [ngrids, nao, ncomp]
+    c->weights.ensure((size_t)std::max<int64_t>(ngrids, 1) * 8, c->counter());
+    copy_in(c, c->weights.p, weights, (size_t)ngrids * 8);
+    const int64_t nf = ngrids * nvar * nvar * (nspin == 1 ? 1 : 4);
+    c->fxcG.ensure((size_t)std::max<int64_t>(nf, 1) * 8, c->counter());
+    copy_in(c, c->fxcG.p, fxc_eff, (size_t)nf * 8);
+    check_finite(c, c->phiG.as<double>(), ngrids * nao * 4, "ao");
+    check_finite(c, c->fxcG.as<double>(), nf, "fxc_eff");
+    (void)batch_offsets;
+    (void)nbatch;  // the dense path chunks the points itself
+    c->phi.release();
+    c->xc_batches.clear();
+    c->xc_plans.clear();
+    c->ngrids = ngrids;
+    c->xc_nspin = nspin;
+    c->xc_den = den_type;
+    c->xc_nvar = (int)nvar;
+    c->has_xc = true;
+    c->prepared = false;
+    lowp_release(c);
+    CPHF_CUDA(cudaStreamSynchronize(c->stream));
   });
 }
 

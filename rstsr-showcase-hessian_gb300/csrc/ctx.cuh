@@ -74,6 +74,7 @@ struct LowpState {
   XcTcState xctc;              // dense split-FP16 phi for the tensor-core XC response
   XcTcState xctc64;            // dense exact-slice phi for the FP64-accurate XC residual
   DevBuf phi32;
+  DevBuf phiG32, s_gket, s_grho;  // GGA / meta-GGA XC in FP32
   DevBuf s_c1, s_resp, s_T, s_W, s_d, s_ket, s_rho, s_y, s_x, s_Thi, s_Tlo, s_acc;
   DevBuf err;                  // device error flag of the tensor-core kernels (bounded waits)
   double sA = 1.0;             // power-of-two scale of the FP16 cderi planes
@@ -107,6 +108,7 @@ struct SpinState {
   // split-precision copies (mixed path)
   DevBuf C32, Z32, O32, aobra32;
   DevBuf iaia;    // [nvir, nocc] FP32: RI diagonal (ia|ia), feature of the learned guess
+  DevBuf aobG, aobG32;  // [ngrids, nocc, 4] phi_c Cocc (GGA / meta-GGA XC), FP64 / FP32
 };
 
 struct XcBatch {
@@ -214,6 +216,11 @@ struct cphf_ctx {
   cphf::DevBuf phi, weights, fxc;  // phi: batch blocks [npts_b, nwin_b] (grid fastest)
   cphf::DevBuf phi32;
   std::vector<std::unique_ptr<cphf::XcPlan>> xc_plans;  // chunk plans, one per (precision, nb, nocc)
+  int xc_den = 0;     // density type: 0 RHO (LDA), 1 SIGMA (GGA), 2 TAU (meta-GGA)
+  int xc_nvar = 1;    // XCDenType::num_nvar (src/xceff/flags.rs:33-40)
+  cphf::DevBuf phiG;  // GGA / meta-GGA: AO values and gradients [ngrids, nao, 4] FP64
+  cphf::DevBuf fxcG;  // GGA / meta-GGA: fxc_eff [ngrids, nvar, nvar] or [ngrids, nvar, 2, nvar, 2]
+  cphf::DevBuf s_gket, s_grho;  // GGA / meta-GGA chunk scratch (FP64)
 
   // prepared orbitals
   bool prepared = false;

@@ -18,6 +18,7 @@
 #include "mlp.cuh"
 #include "tc_gemm.cuh"
 #include "tc_ozaki.cuh"
+#include "xc_gga.cuh"
 #include "xc_grouped.cuh"
 #include "xc_tc.cuh"
 
@@ -52,15 +53,26 @@ void lowp_prepare(cphf_ctx* c) {
       sp.O32.ensure((size_t)sp.nocc * sp.nocc * naux * 4, c->counter());
       launch_to_f32(sp.O.as<double>(), sp.nocc * sp.nocc * naux, sp.O32.as<float>(), c->stream);
     }
-    if (c->has_xc) {
+    if (c->has_xc && c->xc_den == 0) {
       sp.aobra32.ensure((size_t)c->ngrids * std::max<int64_t>(sp.nocc, 1) * 4, c->counter());
       launch_to_f32(sp.aobra.as<double>(), c->ngrids * sp.nocc, sp.aobra32.as<float>(), c->stream);
     }
   }
-  if (c->has_xc) {
+  if (c->has_xc && c->xc_den == 0) {
     const int64_t tot = c->phi.bytes / 8;
     L.phi32.ensure((size_t)std::max<int64_t>(tot, 1) * 4, c->counter());
     launch_to_f32(c->phi.as<double>(), tot, L.phi32.as<float>(), c->stream);
+  }
+  if (c->has_xc && c->xc_den != 0) {  // GGA / meta-GGA: FP32 copies of phi and phi_c Cocc
+    const int64_t tot = c->ngrids * c->nao * 4;
+    L.phiG32.ensure((size_t)std::max<int64_t>(tot, 1) * 4, c->counter());
+    launch_to_f32(c->phiG.as<double>(), tot, L.phiG32.as<float>(), c->stream);
+    for (int s = 0; s < c->nspin; ++s) {
+      SpinState& sp = c->spin[s];
+      const int64_t n4 = c->ngrids * sp.nocc * 4;
+      sp.aobG32.ensure((size_t)std::max<int64_t>(n4, 1) * 4, c->counter());
+      launch_to_f32(sp.aobG.as<double>(), n4, sp.aobG32.as<float>(), c->stream);
+    }
   }
   // Chunk budget of the K term's T / W intermediates: up to 8 GiB, at most a quarter of the
   // memory still free once the resident operand planes are in place (fewer, longer launches).
@@ -187,6 +199,11 @@ static void rijk_response_lowp(cphf_ctx* c, float* const* bra, int64_t nb, float
 
 static void xc_response_lowp(cphf_ctx* c, float* const* bra, int64_t nb, float* const* out, bool accumulate) {
   LowpState& L = *c->lowp;
+  if (c->xc_den != 0) {  // GGA / meta-GGA on the CUDA cores in FP32
+    const float* aob[2] = {c->spin[0].aobG32.as<float>(), c->nspin > 1 ? c->spin[1].aobG32.as<float>() : nullptr};
+    xc_response_gga<float>(c, bra, nb, out, accumulate, L.phiG32.as<float>(), aob, L.s_gket, L.s_grho);
+    return;
+  }
   if (L.use_tc) {
     xc_response_tc(c, bra, nb, out, accumulate);
     return;
@@ -347,7 +364,7 @@ AccurateScope::AccurateScope(cphf_ctx* ctx, int mode, bool correction) : c(ctx) 
   const bool tc = c->lowp && c->lowp->use_tc && oz_available(c);
   c->f64_emulate = mode != 0;
   c->oz_kterm = mode == 2 && c->has_rijk && tc && oz_supported(c);
-  c->oz_xc = mode == 2 && c->has_xc && tc;
+  c->oz_xc = mode == 2 && c->has_xc && c->xc_den == 0 && tc;  // the tensor-core XC covers LDA
   c->oz_correction = correction && c->oz_kterm;
   c->f32_correction = c->oz_correction;  // the correction's J, C x and C^T r GEMMs to ~1e-7 of it
   // mode 2 without any tensor-core contraction available is the double-float operator

@@ -18,12 +18,17 @@
 
 #include "ctx.cuh"
 #include "kernels.cuh"
+#include "xc_gga.cuh"
 #include "xc_grouped.cuh"
 #include "xc_tc.cuh"
 
 namespace cphf {
 
 void xc_prepare(cphf_ctx* c) {
+  if (c->xc_den != 0) {
+    xc_gga_prepare(c);
+    return;
+  }
   for (int s = 0; s < c->nspin; ++s) {
     SpinState& sp = c->spin[s];
     const int64_t no = sp.nocc;
@@ -47,6 +52,11 @@ void xc_prepare(cphf_ctx* c) {
 
 void xc_response_fp64(cphf_ctx* c, const double* const* bra, int64_t nb, double* const* out,
                       bool accumulate) {
+  if (c->xc_den != 0) {  // GGA / meta-GGA (double-float GEMMs inside the FP64-accurate residual)
+    const double* aob[2] = {c->spin[0].aobG.as<double>(), c->nspin > 1 ? c->spin[1].aobG.as<double>() : nullptr};
+    xc_response_gga<double>(c, bra, nb, out, accumulate, c->phiG.as<double>(), aob, c->s_gket, c->s_grho);
+    return;
+  }
   if (c->oz_xc && c->lowp) {
     xc_response_tc64(c, bra, nb, out, accumulate);
     return;

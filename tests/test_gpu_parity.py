@@ -501,3 +501,78 @@ def test_compute_dimless_cphf_rhs_golden(name):
                                                         None, g["s1ao"])
     assert rel_err(rhs0 if nspin == 1 else rhs0[0], r_ref) < 1e-12
     assert rel_err(f10 if nspin == 1 else f10[0], f_ref) < 1e-12
+
+
+GRID_MG = dict(nao=56, naux=170, nocc=(8,), natm=4, decay=10.0, grid=True, points=(500, 900), window=18)
+GRID_MG_U = dict(nao=52, naux=160, nocc=(7, 6), natm=4, decay=10.0, grid=True, points=(500, 900), window=18)
+
+
+def _mgga_ctx(s, den, precision="fp64", coupling=0.1, fxc_scale=1.0, **cfg):
+    ao, fxc = synth.make_mgga_grid(s.grid, den, seed=41, nspin=s.nspin, coupling=coupling)
+    fxc = fxc * fxc_scale
+    ctx = Context(precision=precision, **cfg)
+    ctx.set_cderi(s.cderi, s.scale_j, s.scale_k)
+    ctx.set_grid_ex(den, ao, s.grid.weights, fxc, s.nspin)
+    if s.nspin == 1:
+        ctx.make_response_preparation(s.mo_coeff[0], s.mo_occ[0], s.mo_energy[0])
+    else:
+        ctx.make_response_preparation(s.mo_coeff, s.mo_occ, s.mo_energy)
+    return ctx, ao, fxc
+
+
+@pytest.mark.parametrize("dims,den", [(GRID_MG, "sigma"), (GRID_MG, "tau"), (GRID_MG_U, "sigma"), (GRID_MG_U, "tau")])
+def test_xc_gga_mgga_response(dims, den):
+    """SIGMA (GGA) and TAU (meta-GGA) XC response of the plugin against the oracle's restatement
+    of pure_eval_rho.rs:289-316 / pure_xcpot.rs:335-351 (1e-12), and the split-precision form."""
+    s = synth.make_system(dims, seed=40)
+    ctx, ao, fxc = _mgga_ctx(s, den, xc_chunk_points=777)   # ragged point chunks
+    rng = np.random.default_rng(42)
+    g = s.grid
+    if s.nspin == 1:
+        bra = rng.standard_normal((s.nao, s.nocc[0], 5))
+        ref = [xc.rks_response_bra_mgga(ao, g.weights, fxc, bra, s.mo_coeff[0][:, :s.nocc[0]], den)]
+        got = [ctx.get_response_bra(bra, plugin="xc")]
+    else:
+        bra = [rng.standard_normal((s.nao, s.nocc[t], 5)) for t in range(2)]
+        ref = xc.uks_response_bra_mgga(ao, g.weights, fxc, bra, [s.mo_coeff[t][:, :s.nocc[t]] for t in range(2)], den)
+        got = ctx.get_response_bra(bra, plugin="xc")
+    for a, b in zip(got, ref):
+        assert rel_err(a, b) < 1e-12
+    lp, _, _ = _mgga_ctx(s, den, precision="mixed")
+    mo1 = [rng.standard_normal((s.nao, s.nocc[t], 4)) for t in range(s.nspin)]
+    arg = (lambda v: v[0]) if s.nspin == 1 else (lambda v: v)
+    r64 = ctx.response_dimless_cphf(arg(mo1))
+    rlp = lp.response_dimless_cphf_lowp(arg(mo1))
+    for a, b in zip([rlp] if s.nspin == 1 else rlp, [r64] if s.nspin == 1 else r64):
+        assert rel_err(a, b) < LOWP_TOL
+
+
+def test_xc_set_grid_ex_rho_is_lda():
+    """den_type RHO through the general entry point is the LDA plugin on component 0."""
+    s = synth.make_system(GRID_R, seed=43)
+    g = s.grid
+    ctx = make_ctx(s)
+    ex = Context()
+    ex.set_cderi(s.cderi, s.scale_j, s.scale_k)
+    ao4 = np.asfortranarray(np.stack([g.ao] * 4, axis=2))
+    ex.set_grid_ex("rho", ao4, g.weights, g.fxc, 1, g.atom_offsets)
+    ex.make_response_preparation(s.mo_coeff[0], s.mo_occ[0], s.mo_energy[0])
+    bra = np.random.default_rng(44).standard_normal((s.nao, s.nocc[0], 3))
+    assert rel_err(ex.get_response_bra(bra, plugin="xc"), ctx.get_response_bra(bra, plugin="xc")) < 1e-13
+
+
+@pytest.mark.parametrize("dims", [GRID_MG, GRID_MG_U])
+def test_mixed_solve_gga(dims):
+    """Mixed-precision CPKS solve with a GGA kernel: the solve's own residual and the native FP64
+    residual both below 1e-8, U1 within 1e-7 of the plain FP64 solve."""
+    s = synth.make_system(dims, seed=45)
+    rhs = s.rhs[0] if s.nspin == 1 else s.rhs
+    c64, _, _ = _mgga_ctx(s, "sigma", fxc_scale=0.5, cphf_tol=1e-10, cphf_lindep=1e-22)
+    x64 = c64.solve_dimless_cphf(rhs)
+    cmx, _, _ = _mgga_ctx(s, "sigma", precision="mixed", fxc_scale=0.5)
+    xmx = cmx.solve_dimless_cphf(rhs)
+    assert cmx.last_stats["residual_max"] < 1e-8
+    res64, _ = _max_col_residual(c64, s, xmx)
+    assert res64 < 1e-8
+    for a, b in zip([xmx] if s.nspin == 1 else xmx, [x64] if s.nspin == 1 else x64):
+        assert np.abs(a - b).max() < 1e-7
