@@ -568,6 +568,166 @@ __global__ void __launch_bounds__(320, PR::NACC == 4 ? 1 : 2)
   if (warp == 1) tmem_dealloc(tmem, 2 * ACC);
 }
 
+// Inner T generation with the bra tile resident (split FP16, K = nocc <= 128): one CTA per
+// (row tile of (nu, a), range of aux functions).  The A tile -- every K block of the bra
+// rows, both planes -- is loaded once and stays in shared memory; only O_P's 128-row tile
+// (all i of a column, N = 128 >= nocc) streams through a 2-stage ring (98 KB in all, two CTAs
+// per SM).  Double-buffered TMEM accumulators (2 x 128 columns) let the epilogue of aux
+// function p (FP16 hi / lo planes of T * tscale, 8 warps of 64 columns each) overlap the MMAs
+// of p + 1.  Warp 0: TMA producer, warp 1: MMA issuer and TMEM owner, warps 2-9: epilogue.
+struct ResT {
+  static constexpr int BN = 128, STAGES = 2, MAX_KB = 4, THREADS = 320, EPI_WARPS = 8;
+  static constexpr int A_TILE = BM * BK * 2;            // 8 KB: one K block of one plane
+  static constexpr int B_TILE = BN * BK * 2;            // 8 KB
+  static constexpr int A_BYTES = MAX_KB * 2 * A_TILE;   // 64 KB resident
+  static constexpr int STAGE_BYTES = 2 * B_TILE;        // hi + lo of one K block of O_P
+  static constexpr int SMEM_BYTES = A_BYTES + STAGES * STAGE_BYTES + 1024 + 1024;
+};
+
+__global__ void __launch_bounds__(320, 2)
+    tc_tgen_resident_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB,
+                            OzArgs args) {
+  constexpr int STAGES = ResT::STAGES, BN = ResT::BN;
+  constexpr uint32_t ACC = BN;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* ares = smem;
+  uint8_t* ring = smem + ResT::A_BYTES;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(ring + STAGES * ResT::STAGE_BYTES);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 6);
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES);
+  const uint32_t accf0 = smem_u32(bars + 2 * STAGES), acce0 = smem_u32(bars + 2 * STAGES + 2);
+  const uint32_t done = smem_u32(bars + 2 * STAGES + 4), abar = smem_u32(bars + 2 * STAGES + 5);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * BM;
+  const int p_begin = blockIdx.x * args.p_per_cta;
+  const int nP = min(args.np - p_begin, args.p_per_cta);
+  const int nkb = args.nkb;  // <= MAX_KB (host checks)
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(accf0 + 8 * b, 1);
+      mbar_init(acce0 + 8 * b, ResT::EPI_WARPS);
+    }
+    mbar_init(done, 1);
+    mbar_init(abar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) tmem_alloc(smem_u32(tmem_slot), 2 * ACC);
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  if (nP > 0) {
+    if (warp == 0 && lane == 0) {
+      // resident A: every K block of both planes, once
+      mbar_expect_tx(abar, (uint32_t)(nkb * 2 * ResT::A_TILE));
+      for (int kb = 0; kb < nkb; ++kb)
+        for (int t = 0; t < 2; ++t)
+          tma_load_3d(smem_u32(ares + (kb * 2 + t) * ResT::A_TILE), &mA, abar, kb * BK, m0, t * args.a_depth + args.a_off);
+      // O_P tiles of the aux range through the ring
+      const int total = nP * nkb;
+      int issued = 0;
+      for (int it = 0; it < total; ++it) {
+        const int s = it % STAGES;
+        if (!mbar_wait(empty0 + 8 * s, ((it / STAGES) & 1) ^ 1, args.err)) break;
+        issued = it + 1;
+        const uint32_t full = full0 + 8 * s;
+        mbar_expect_tx(full, ResT::STAGE_BYTES);
+        const int P = p_begin + it / nkb;
+        const int k0 = (it % nkb) * BK;
+        const uint32_t st = smem_u32(ring + s * ResT::STAGE_BYTES);
+        for (int t = 0; t < 2; ++t) tma_load_3d(st + t * ResT::B_TILE, &mB, full, k0, 0, t * args.b_depth + args.b_off + P);
+      }
+      for (int it = max(0, issued - STAGES); it < issued; ++it)
+        mbar_wait(full0 + 8 * (it % STAGES), (it / STAGES) & 1, nullptr);
+      mbar_wait(abar, 0, nullptr);  // the resident copies have landed before the CTA may exit
+    } else if (warp == 1 && lane == 0) {
+      constexpr uint32_t idesc = instr_desc_f16(BM, BN, false);
+      bool ok = mbar_wait(abar, 0, args.err);
+      fence_after_sync();
+      for (int p = 0; p < nP && ok; ++p) {
+        const int b = p & 1;
+        if (!mbar_wait(acce0 + 8 * b, ((p >> 1) & 1) ^ 1, args.err)) break;
+        fence_after_sync();
+        const uint32_t acc_base = tmem + (uint32_t)b * ACC;
+        for (int kb = 0; kb < nkb; ++kb) {
+          const int it = p * nkb + kb;
+          const int s = it % STAGES;
+          if (!mbar_wait(full0 + 8 * s, (it / STAGES) & 1, args.err)) { ok = false; break; }
+          fence_after_sync();
+          const uint32_t ah = smem_u32(ares + (kb * 2 + 0) * ResT::A_TILE), al = ah + ResT::A_TILE;
+          const uint32_t bh = smem_u32(ring + s * ResT::STAGE_BYTES), bl = bh + ResT::B_TILE;
+#pragma unroll
+          for (int k = 0; k < BK / 16; ++k) {
+            const uint64_t dk = (uint64_t)((k * 32) >> 4);
+            mma_f16(acc_base, smem_desc<64>(ah) + dk, smem_desc<64>(bh) + dk, idesc, (kb > 0 || k > 0) ? 1u : 0u);
+            mma_f16(acc_base, smem_desc<64>(ah) + dk, smem_desc<64>(bl) + dk, idesc, 1u);
+            mma_f16(acc_base, smem_desc<64>(al) + dk, smem_desc<64>(bh) + dk, idesc, 1u);
+          }
+          mma_commit(empty0 + 8 * s);
+        }
+        if (ok) mma_commit(accf0 + 8 * b);
+      }
+      mma_commit(done);
+      mbar_wait(done, 0, nullptr);
+    } else if (warp >= 2) {
+      // epilogue: TMEM lane quarter q, columns [64 h, 64 h + 64)
+      const int q = warp & 3;
+      const int h = (warp - 2) >> 2;
+      const int row = m0 + q * 32 + lane;
+      const bool row_ok = row < args.M;
+      int erow = 0;
+      int64_t base = 0;
+      if (row_ok) {
+        erow = args.e_row[row] - 2 * Split2::EOFF;
+        base = (row % args.m_div) * args.s_m1 + (row / args.m_div) * args.s_m2;
+      }
+      for (int p = 0; p < nP; ++p) {
+        const int b = p & 1;
+        if (!__all_sync(0xffffffffu, mbar_wait(accf0 + 8 * b, (p >> 1) & 1, args.err))) break;
+        fence_after_sync();
+        const int Pl = p_begin + p;
+        const int64_t pbase = base + (int64_t)Pl * args.s_p;
+        const float ts = *args.tscale;
+#pragma unroll
+        for (int cc = 0; cc < 2; ++cc) {
+          const int c0 = h * 64 + cc * 32;
+          float v[32];
+          tmem_ld32(tmem + (uint32_t)b * ACC + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+          const int ncol = c0 + lane;
+          const int ec = ncol < args.N ? args.e_col[(int64_t)(args.b_off + Pl) * args.N + ncol] : 0;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int n = c0 + j;
+            const float f = pow2f(erow + __shfl_sync(0xffffffffu, ec, j));
+            if (row_ok && n < args.N) {
+              const float x = (v[j] * f) * ts;
+              const __half hh = __float2half_rn(x);
+              const int64_t off = pbase + n * args.s_n;
+              reinterpret_cast<__half*>(args.out)[off] = hh;
+              reinterpret_cast<__half*>(args.out_lo)[off] = __float2half_rn(x - __half2float(hh));
+            }
+          }
+        }
+        fence_before_sync();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(acce0 + 8 * b);
+      }
+    }
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  if (warp == 1) tmem_dealloc(tmem, 2 * ACC);
+}
+
 // Generic row slicer: row r, element k at src[(r % rdiv) rs1 + (r / rdiv) rs2 + k ks]
 // (rdiv = 0: r rs1 + k ks); one warp per row: exponent of the row max, then the six slices
 // to dst[t plane + r ld + k]; e_out[r] = exponent, scale_out[r] = 2^exponent (if non-null).
@@ -904,6 +1064,44 @@ void launch_batched(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, c
   launch_batched_raw<PR, EPI>(c, mA, mB, a, best);
 }
 
+bool res_attr_ok() {
+  static int state = -1;
+  if (state < 0) {
+    state = cudaFuncSetAttribute(tc_tgen_resident_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 ResT::SMEM_BYTES) == cudaSuccess ? 1 : 0;
+    if (!state) cudaGetLastError();
+  }
+  return state == 1;
+}
+
+void launch_tgen_resident_raw(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, OzArgs a, int waves) {
+  const int64_t tiles = a.m_tiles;
+  if (tiles > 65535) throw Error(CPHF_ERR_ARG, "tensor-core T generation: grid too large");
+  a.p_per_cta = (int)std::max<int64_t>(1, std::min<int64_t>(a.np, a.np * tiles / (waves * (int64_t)c->num_sms)));
+  const dim3 grid((unsigned)div_up(a.np, a.p_per_cta), (unsigned)tiles);
+  tc_tgen_resident_kernel<<<grid, ResT::THREADS, ResT::SMEM_BYTES, c->stream>>>(mA, mB, a);
+  count_launch();
+  CPHF_CUDA(cudaGetLastError());
+}
+
+// aux functions per CTA from the waves of CTAs over the SMs, tuned once per shape (every
+// candidate writes the same planes, so the last one's output stands)
+void launch_tgen_resident(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, const OzArgs& a) {
+  const TuneKey key{9000, a.M, a.N, a.nkb, a.np};
+  auto& tab = tune_table();
+  int best = 2;
+  if (!tab.find(key, best) && !capturing(c->stream)) {
+    float best_ms = 0.f;
+    for (int w : {2, 4, 8}) {
+      const float ms = time_launch(c->stream, [&] { launch_tgen_resident_raw(c, mA, mB, a, w); });
+      if (best_ms == 0.f || ms < best_ms) best_ms = ms, best = w;
+    }
+    tab.put(key, best);
+    return;
+  }
+  launch_tgen_resident_raw(c, mA, mB, a, best);
+}
+
 OzArgs base_args(OzState& z, int M, int N) {
   OzArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -1231,7 +1429,13 @@ void lp_tgen_planes(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int
   tbound_kernel<<<1, 256, 0, c->stream>>>(z.braS.as<unsigned>(), z.spin[s].Omax.as<unsigned>() + P0, npc, mx);
   count_launch();
   launch_t_scale(mx, sA, alpha, scale, c->stream);
-  launch_batched<Split2, EPI_SPLIT16>(c, mBt, mO, a);
+  if (a.nkb <= ResT::MAX_KB && no <= ResT::BN && res_attr_ok()) {
+    // bra tile resident, all i of a column in one 128-wide tile
+    const CUtensorMap mO128 = make_map(z.spin[s].O.p, no, no, S2 * naux, ldj, ResT::BN, false);
+    launch_tgen_resident(c, mBt, mO128, a);
+  } else {
+    launch_batched<Split2, EPI_SPLIT16>(c, mBt, mO, a);
+  }
 }
 
 void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t nb, double alpha, float* out,
