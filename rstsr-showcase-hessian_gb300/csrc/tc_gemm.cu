@@ -53,7 +53,9 @@ struct TcArgs {
   int p_per_cta;    // aux functions per CTA (P split)
   int pA0;          // global aux index of the chunk's first function (A coordinate)
   int m_tiles;
-  const float* scale;  // device: alpha / (sA * sT)
+  const float* scale;  // device: alpha / (sA * sT), or null (1)
+  const double* rowscale;  // per-row / per-column factors of the result (null: 1), the scales of
+  const double* colscale;  // row- / column-scaled operand planes
   int* err;
 };
 
@@ -143,16 +145,23 @@ __global__ void __launch_bounds__(128, 1)
     const bool have = __all_sync(0xffffffffu, mbar_wait(accum, 0, args.err) && *(volatile int*)args.err == 0);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (have) {
-      const float scale = *args.scale;
       const int row = m0 + warp * 32 + lane;
+      const float scale = (args.scale ? *args.scale : 1.f) *
+                          ((args.rowscale && row < args.M) ? (float)args.rowscale[row] : 1.f);
       for (int c = 0; c < BN / 32; ++c) {
         float v[32];
         tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), v);
+        // the chunk's 32 column factors: one load per lane, broadcast by shuffles
+        const int nl = n0 + c * 32 + lane;
+        const float csl = (args.colscale && nl < args.N) ? (float)args.colscale[nl] : 1.f;
+        float cs[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j) cs[j] = __shfl_sync(0xffffffffu, csl, j);
         if (row < args.M) {
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             const int n = n0 + c * 32 + j;
-            if (n < args.N) atomicAdd(args.out + row + args.ld_out * (int64_t)n, scale * v[j]);
+            if (n < args.N) atomicAdd(args.out + row + args.ld_out * (int64_t)n, scale * cs[j] * v[j]);
           }
         }
       }
@@ -340,6 +349,8 @@ void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, 
     a.pA0 = (int)P0;
     a.m_tiles = m_tiles;
     a.scale = scale + 1;
+    a.rowscale = nullptr;
+    a.colscale = nullptr;
     a.err = L.err.as<int>();
     dim3 grid((unsigned)(m_tiles * n_tiles), (unsigned)div_up(npc, ppc));
     // algorithmic FLOPs of the contraction (the tensor pipe executes three split products);
@@ -349,6 +360,38 @@ void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, 
     count_launch();
     CPHF_CUDA(cudaGetLastError());
   }
+}
+
+void tc_planes_term(cphf_ctx* c, const __half* a_hi, const __half* a_lo, int64_t a_depth, int64_t a_off,
+                    const __half* b_hi, const __half* b_lo, int64_t npc, int64_t M, int64_t N, int64_t K, int64_t ld,
+                    const double* rowscale, const double* colscale, float* out, int64_t ld_out, int* err) {
+  if (M <= 0 || N <= 0 || K <= 0 || npc <= 0) return;
+  const int m_tiles = (int)div_up(M, BM), n_tiles = (int)div_up(N, BN);
+  const CUtensorMap mAh = make_map(a_hi, K, M, a_depth, ld, BM);
+  const CUtensorMap mAl = make_map(a_lo, K, M, a_depth, ld, BM);
+  const CUtensorMap mBh = make_map(b_hi, K, N, npc, ld, BN);
+  const CUtensorMap mBl = make_map(b_lo, K, N, npc, ld, BN);
+  TcArgs a;
+  a.out = out;
+  a.ld_out = ld_out;
+  a.M = (int)M;
+  a.N = (int)N;
+  a.nkb = (int)div_up(K, BK);
+  a.np = (int)npc;
+  // one K range per tile unless the tiles alone leave SMs idle
+  const int64_t tiles = (int64_t)m_tiles * n_tiles;
+  const int64_t ranges = std::max<int64_t>(1, std::min<int64_t>(npc, div_up(2 * (int64_t)c->num_sms, tiles)));
+  a.p_per_cta = (int)div_up(npc, ranges);
+  a.pA0 = (int)a_off;
+  a.m_tiles = m_tiles;
+  a.scale = nullptr;
+  a.rowscale = rowscale;
+  a.colscale = colscale;
+  a.err = err;
+  dim3 grid((unsigned)tiles, (unsigned)div_up(npc, a.p_per_cta));
+  tc_term1_kernel<<<grid, 128, SMEM_BYTES, c->stream>>>(mAh, mAl, mBh, mBl, a);
+  count_launch();
+  CPHF_CUDA(cudaGetLastError());
 }
 
 }  // namespace cphf

@@ -25,6 +25,12 @@ using TPlanes =
 // `tplanes` (alpha enters through scale[1])
 void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, int64_t nocc, int64_t nb,
                 float* out, DevBuf& Thi, DevBuf& Tlo, const TPlanes& tplanes);
+// out[m + ld_out n] += rowscale[m] colscale[n] sum_{Pl < npc} sum_{k < K} A_(a_off+Pl)[m, k] B_Pl[n, k]
+// over split-FP16 planes (hi / lo, three products) with the term-1 kernel's 256-wide tiles:
+// A planes [a_depth][M][ld] per plane array, B planes [npc][N][ld]; FP32 atomics into out.
+void tc_planes_term(cphf_ctx* c, const __half* a_hi, const __half* a_lo, int64_t a_depth, int64_t a_off,
+                    const __half* b_hi, const __half* b_lo, int64_t npc, int64_t M, int64_t N, int64_t K, int64_t ld,
+                    const double* rowscale, const double* colscale, float* out, int64_t ld_out, int* err);
 // scale[0] = 2^(14 - e) for max |T| = *mx < 2^e, scale[1] = alpha / (sA scale[0])
 void launch_t_scale(const unsigned* mx, float sA, float alpha, float* scale, cudaStream_t stream);
 

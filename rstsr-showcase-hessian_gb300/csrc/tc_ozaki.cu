@@ -1480,23 +1480,13 @@ void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t
     count_launch(3);
   }
   {
-    // term 2: out[mu, n] += alpha sum_{P, j} Z_P[mu, j] W_P[j, n]
-    const CUtensorMap mZt = make_map(os.Zt.p, no, nao, S2 * naux, ldj, BM, false);
-    const CUtensorMap mW = make_map(z.Ws.p, no, N, S2 * npc, ldj, BM, false);
-    OzArgs a = base_args(z, (int)nao, (int)N);
-    a.err = err;
-    a.out = out;
-    a.nkb = (int)div_up(no, BK);
-    a.total_kb = (int)(npc * a.nkb);
-    a.a_depth = (int)naux;
-    a.a_off = (int)P0;
-    a.a_per_p = 1;
-    a.b_depth = (int)npc;
-    a.rowscale = os.sZt.as<double>();
-    a.colscale = z.colscale.as<double>();
-    a.ld_out = nao;
+    // term 2: out[mu, n] += alpha sum_{P, j} Z_P[mu, j] W_P[j, n] on the term-1 kernel's 256-wide
+    // tiles (K = j per aux function in 64-wide blocks), rows scaled by Z^T's, columns by W's scales
     ProfScope ps(c, PROF_TC_TERM2, 2.0 * nao * N * no * npc, 2.0 * S2 * no * npc * (nao + N));
-    launch_split<Split2, 128>(c, z, mZt, mW, a);
+    const __half* zt = os.Zt.as<__half>();
+    const __half* ws = z.Ws.as<__half>();
+    tc_planes_term(c, zt, zt + naux * nao * ldj, naux, P0, ws, ws + npc * N * ldj, npc, nao, N, no, ldj,
+                   os.sZt.as<double>(), z.colscale.as<double>(), out, nao, err);
   }
 }
 
