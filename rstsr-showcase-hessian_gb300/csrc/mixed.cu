@@ -442,13 +442,7 @@ bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, d
     // the inner solve's Gram / projection GEMMs in double-float (its operator is ~1e-6 accurate)
     c->f64_emulate = c->cfg.residual_dfloat != 0;
     try {
-      // Later corrections need only bring the residual below the target: relative tolerance
-      // 0.1 residual_tol / |r| (within [inner_tol, 1e-2]) instead of inner_tol; the split
-      // operator's own ~1e-6 error of the correction stays below that either way.
-      KrylovParams pk = p;
-      if (step > 0 && res > 0.0)
-        pk.tol = std::max(c->cfg.inner_tol, std::min(1e-2, 0.1 * c->cfg.residual_tol / res));
-      krylov_device(c, op, rr, g0, n, nset, pk, dlt, st);
+      krylov_device(c, op, rr, g0, n, nset, p, dlt, st);
     } catch (...) {
       c->f64_emulate = false;
       throw;
