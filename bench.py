@@ -50,6 +50,7 @@ WORKLOAD_DESC = {
     "rhf_nao600": "RHF CPHF, RI-JK response: nao=600 naux=2000 nocc=60 nvir=540 nrhs=180 (60 atoms)",
     "rhf_nao24": "RHF CPHF, RI-JK response: nao=24 naux=84 nocc=5 nrhs=12 (4 atoms)",
     "rhf_nao300": "RHF CPHF, RI-JK response: nao=300 naux=1000 nocc=30 nrhs=90 (30 atoms)",
+    "rhf_nao384_occ120": "RHF CPHF, RI-JK response: nao=384 naux=1280 nocc=120 nrhs=36 (12 atoms)",
     "rks_nao600": "RKS CPKS, RI-JK + LDA XC response on ~660k grid points: nao=600 naux=2000 nocc=60 nrhs=180",
     "uks_nao800": "UKS CPKS, RI-JK + LDA XC: nao=800 naux=2700 nocc=80/78 nrhs=240",
 }
@@ -93,7 +94,9 @@ def parse(argv=None):
                    help="only time --reps operator applications of --nb columns (launch lists / captures)")
     p.add_argument("--nb", type=int, default=0, help="--apply-only: columns per application (0: all RHS)")
     p.add_argument("--reps", type=int, default=3, help="--apply-only: applications")
-    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="--apply-only: operator")
+    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "accurate"],
+                   help="--apply-only: operator (accurate: the mixed context's FP64-accurate operator, run by "
+                        "finalize_cphf on all 3 natm perturbations)")
     return p.parse_args(argv)
 
 
@@ -361,12 +364,24 @@ def run_apply_only(args, local):
     from cphf_gb300 import synth
     cphf_gb300.build()
     s = synth.make_system(args.workload, seed=args.seed)
-    nb = args.nb or 3 * s.natm
-    ctx = setup_ctx(cphf_gb300, s, args.precision, local)
+    accurate = args.precision == "accurate"
+    nb = 3 * s.natm if accurate else (args.nb or 3 * s.natm)
+    ctx = setup_ctx(cphf_gb300, s, "mixed" if accurate else args.precision, local)
     rng = np.random.default_rng(args.seed + 1)
     mo1 = [rng.standard_normal((s.nao, s.nocc[t], nb)) for t in range(s.nspin)]
     mo1 = mo1 if s.nspin == 2 else mo1[0]
     op = ctx.response_dimless_cphf_lowp if args.precision == "mixed" else ctx.response_dimless_cphf
+    if accurate:
+        # the split-precision state first (its planes of B feed the exact slices' preparation),
+        # then finalize_cphf, whose response is the FP64-accurate operator on mo1
+        ctx.response_dimless_cphf_lowp(mo1)
+        shp = [(s.nao, s.nocc[t], 3, s.natm) for t in range(s.nspin)]
+        f1 = [rng.standard_normal(sh) for sh in shp]
+        s1 = [rng.standard_normal(sh) for sh in shp]
+        m1 = [m.reshape(sh, order="F") for m, sh in zip(mo1 if s.nspin == 2 else [mo1], shp)]
+        if s.nspin == 1:
+            f1, s1, m1 = f1[0], s1[0], m1[0]
+        op = lambda _: ctx.finalize_cphf(f1, s1, m1)  # noqa: E731
     for r in range(args.reps):
         t0 = time.perf_counter()
         op(mo1)
@@ -604,6 +619,10 @@ def run_gpu(args, world, rank, local):
         "tgen_tcgen05_bf16x4c_exact": "exact BF16 slices in correction precision, 10 slice products",
         "wgen_tcgen05_bf16x4c_exact": "exact BF16 slices in correction precision, 10 slice products",
         "term2_tcgen05_bf16x4c_exact": "exact BF16 slices in correction precision, 10 slice products",
+        "kterm_tcgen05_bf16x3c_exact": "exact BF16 slices in correction precision, 6 slice products",
+        "tgen_tcgen05_bf16x3c_exact": "exact BF16 slices in correction precision, 6 slice products",
+        "wgen_tcgen05_bf16x3c_exact": "exact BF16 slices in correction precision, 6 slice products",
+        "term2_tcgen05_bf16x3c_exact": "exact BF16 slices in correction precision, 6 slice products",
     }
     if dom_name in ("slice_scale_split", "slice_exact"):
         roof = dict(bound="hbm", achieved=dom["bytes"] / dom["ms"] / 1e6, peak=hbm, unit="GB/s",
@@ -635,7 +654,9 @@ def run_gpu(args, world, rank, local):
                 "xc_tcgen05_f16x3": 3, "xc_tcgen05_bf16x6_exact": 21, "tgen_tcgen05_bf16x6_exact": 21,
                 "wgen_tcgen05_bf16x6_exact": 21, "term2_tcgen05_bf16x6_exact": 21,
                 "kterm_tcgen05_bf16x4c_exact": 10, "tgen_tcgen05_bf16x4c_exact": 10,
-                "wgen_tcgen05_bf16x4c_exact": 10, "term2_tcgen05_bf16x4c_exact": 10}.get(dom_name)
+                "wgen_tcgen05_bf16x4c_exact": 10, "term2_tcgen05_bf16x4c_exact": 10,
+                "kterm_tcgen05_bf16x3c_exact": 6, "tgen_tcgen05_bf16x3c_exact": 6,
+                "wgen_tcgen05_bf16x3c_exact": 6, "term2_tcgen05_bf16x3c_exact": 6}.get(dom_name)
     if products and roof.get("peak"):
         roof.update(tensor_executed_tflops=roof["achieved"] * products,
                     tensor_executed_frac=roof["achieved"] * products / roof["peak"])

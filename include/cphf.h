@@ -73,10 +73,12 @@ typedef struct cphf_config {
                                 r -= (I + A_lowp) d (no FP64-accurate application);  1 = recomputed with
                                 the native FP64 operator;  2 (default) = computed with the FP64-accurate
                                 operator of residual_dfloat: with the exact-slice tensor cores (residual_dfloat
-                                = 2) as r -= (I + A) d, the correction d applied in correction precision
-                                (4 BF16 slices per operand, 10 exact-accumulated products, ~2^-24 relative
-                                to |d| where |d| ~ inner_tol |r|), otherwise recomputed in full.  With 1 or 2
-                                the solve returns only after such a max_j ||b_j - (I+A)x_j||_2 < residual_tol. */
+                                = 2) as r -= (I + A) d, the correction d applied in correction precision:
+                                the fewest BF16 slices per operand whose error bound (3 slices, 6
+                                exact-accumulated products: ~2^-12 |r|; 4 slices, 10 products: ~2^-18 |r|)
+                                stays below 0.1 residual_tol, else all six; otherwise recomputed in full.
+                                With 1 or 2 the solve returns only after such a max_j ||b_j - (I+A)x_j||_2
+                                < residual_tol. */
   int32_t fp64_every_step;   /* mixed: FP64 residual after every correction, not only the first (default 0) */
   int64_t xc_chunk_points;   /* grid points per XC chunk (default 0 = 8 GiB of intermediates) */
   int32_t residual_dfloat;   /* mixed: arithmetic of the correction residuals.  0 = native FP64;

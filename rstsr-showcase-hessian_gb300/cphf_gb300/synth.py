@@ -45,6 +45,9 @@ CONFIGS = {
     "rhf_nao600": dict(nao=600, naux=2000, nocc=(60,), natm=60, decay=20.0),
     # half-size case for profiler captures: nao=300, naux=1000, nocc=30, nrhs=90
     "rhf_nao300": dict(nao=300, naux=1000, nocc=(30,), natm=30, decay=20.0),
+    # profiler captures at the evaluation size's nocc (120 = the width of one T tile):
+    # nao=384, naux=1280, nocc=120, nrhs=36 (12 atoms)
+    "rhf_nao384_occ120": dict(nao=384, naux=1280, nocc=(120,), natm=12, decay=20.0),
     # config above plus a ~660k-point LDA grid (60 atoms x 10 AOs)
     "rks_nao600": dict(nao=600, naux=2000, nocc=(60,), natm=60, decay=20.0, grid=True),
     # UHF/UKS: nao=800, naux=2700, nocc 80/78, 240 RHS (80 atoms)

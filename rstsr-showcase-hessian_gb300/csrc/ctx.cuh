@@ -20,7 +20,7 @@ struct OzSpin {
   DevBuf O, eO;        // [6][naux][nocc(i)][ldj] of O_P[j, i], K = j; exponent per (P, i)
   DevBuf Z, eZ;        // [6][naux][nocc(i)][ldk] of Z_P[nu, i], K = nu; exponent per (P, i)
   DevBuf Zt, sZt, eZt; // [6][naux][nao(mu)][ldj] of Z_P[mu, j], K = j; scale per mu over (j, P)
-  DevBuf Omax;         // split FP16: max |O_P| per aux function (float bits), for the T bound
+  DevBuf Omax, Zmax;   // split FP16: max |O_P|, max |Z_P| per aux function (float bits), for the T / W bounds
   int64_t ldj = 0;     // padded K = nocc rows
   bool ready = false;
 };
@@ -29,7 +29,7 @@ struct OzState {
   DevBuf rowscale, e_row, mx;  // per-row power-of-two scales of A
   OzSpin spin[2];
   // per-call scratch: bra slices (both K orders), T / Wt staging (FP32 pairs) and slices
-  DevBuf braw, ebraw, brat, ebrat, T, B, W, Ws, braS;
+  DevBuf braw, ebraw, brat, ebrat, T, B, W, Ws, braS, braWS, wsc;
   DevBuf colscale, e_col, mxc, err, tune_out;
   int64_t ldk = 0;
   bool ready = false;
@@ -186,7 +186,11 @@ enum ProfClass {
   PROF_OZC_WGEN = 19,
   PROF_OZC_TERM2 = 20,
   PROF_SLICE_EXACT = 21,
-  PROF_NCLASS = 22
+  PROF_OZC3_KTERM = 22,
+  PROF_OZC3_TGEN = 23,
+  PROF_OZC3_WGEN = 24,
+  PROF_OZC3_TERM2 = 25,
+  PROF_NCLASS = 26
 };
 extern const char* const kProfNames[PROF_NCLASS];
 
@@ -237,7 +241,7 @@ struct cphf_ctx {
   cphf::Profiler prof;
   bool f64_emulate = false;  // route the FP64 GEMMs through the double-float kernel
   bool oz_kterm = false;     // FP64 K term 1 on the tensor cores (exact BF16 slices)
-  bool oz_correction = false;  // ... in correction precision (slices 0-3, 10 products)
+  int oz_correction = 0;       // ... in correction precision: 0 off, else the slices read (3 or 4)
   bool f32_correction = false; // FP64 GEMMs of a correction-precision application run in FP32
   bool oz_xc = false;        // FP64 XC response on the tensor cores (exact BF16 slices)
 
@@ -317,7 +321,7 @@ void lowp_release(cphf_ctx* c);
 struct AccurateScope {
   cphf_ctx* c;
   int used = 0;
-  AccurateScope(cphf_ctx* ctx, int mode, bool correction = false);
+  AccurateScope(cphf_ctx* ctx, int mode, int correction_slices = 0);
   ~AccurateScope();
   AccurateScope(const AccurateScope&) = delete;
   AccurateScope& operator=(const AccurateScope&) = delete;

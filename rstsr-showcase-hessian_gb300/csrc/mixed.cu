@@ -146,9 +146,11 @@ static void rijk_response_lowp(cphf_ctx* c, float* const* bra, int64_t nb, float
                      lp_tgen_planes(c, L.lp, s, P0, npc, nb, L.ldk, hi, lo, mx, scale, (float)L.sA,
                                     (float)-c->scale_k, err);
                    });
-        // W / term-2 chunk: FP32 W staging and its two FP16 planes, nocc-wide rows, within the budget
+        // W / term-2 chunk: W's two FP16 planes, nocc-wide rows, within the budget and with
+        // 32-bit plane offsets
         const int64_t ldj = (no + 7) / 8 * 8;
-        const int64_t np_w = std::max<int64_t>(1, std::min<int64_t>(naux, L.budget / std::max<int64_t>(8 * no * nb * ldj, 1)));
+        int64_t np_w = std::max<int64_t>(1, std::min<int64_t>(naux, L.budget / std::max<int64_t>(4 * no * nb * ldj, 1)));
+        np_w = std::max<int64_t>(1, std::min<int64_t>(np_w, ((int64_t)INT32_MAX - 1) / std::max<int64_t>(no * nb * ldj, 1)));
         for (int64_t P0 = 0; P0 < naux; P0 += np_w)
           lp_w_term2(c, L.lp, s, P0, std::min<int64_t>(np_w, naux - P0), nb, -c->scale_k, out[s], err);
         continue;
@@ -360,13 +362,13 @@ void lowp_apply(cphf_ctx* c, const double* x, int64_t nb, double* y) {
   L.graphs.push_back(g);
 }
 
-AccurateScope::AccurateScope(cphf_ctx* ctx, int mode, bool correction) : c(ctx) {
+AccurateScope::AccurateScope(cphf_ctx* ctx, int mode, int correction_slices) : c(ctx) {
   const bool tc = c->lowp && c->lowp->use_tc && oz_available(c);
   c->f64_emulate = mode != 0;
   c->oz_kterm = mode == 2 && c->has_rijk && tc && oz_supported(c);
   c->oz_xc = mode == 2 && c->has_xc && c->xc_den == 0 && tc;  // the tensor-core XC covers LDA
-  c->oz_correction = correction && c->oz_kterm;
-  c->f32_correction = c->oz_correction;  // the correction's J, C x and C^T r GEMMs to ~1e-7 of it
+  c->oz_correction = c->oz_kterm ? correction_slices : 0;
+  c->f32_correction = c->oz_correction != 0;  // the correction's J, C x and C^T r GEMMs to ~1e-7 of it
   // mode 2 without any tensor-core contraction available is the double-float operator
   used = mode == 2 && !(c->oz_kterm || c->oz_xc) ? 1 : mode;
 }
@@ -375,7 +377,7 @@ AccurateScope::~AccurateScope() {
   c->f64_emulate = false;
   c->oz_kterm = false;
   c->oz_xc = false;
-  c->oz_correction = false;
+  c->oz_correction = 0;
   c->f32_correction = false;
 }
 
@@ -454,13 +456,17 @@ bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, d
     const char* how;
     if (step > 0 && c->cfg.verify_residual == 2 && first_mode == 2 && !c->cfg.fp64_every_step &&
         st->residual_mode != 3) {
-      // r -= (I + A) d with the exact-slice operator in correction precision: d is a correction
-      // of relative size ~inner accuracy, so 4 BF16 slices per operand (10 exact-accumulated
-      // products, ~2^-24 relative to |d|) keep this term far below the recomputed residual's
-      // own ~2^-34 |x|; r stays a computed residual, not a split-precision estimate.
+      // r -= (I + A) d with the exact-slice operator in correction precision: d solves
+      // (I + A) d = r, so |(I + A) d| ~ |r|, and an operator accurate to eps relative to |A| |d|
+      // adds ~eps |r| (with a margin of 16 for |A| |(I + A)^-1|).  The fewest slices whose error
+      // stays below a tenth of residual_tol: 3 (6 exact-accumulated products, eps ~2^-16), 4
+      // (10, ~2^-22), else all six; r stays a computed residual with a worst-case bound, not
+      // a split-precision estimate.
+      const double tenth = 0.1 * c->cfg.residual_tol;
+      const int slices = res * 0x1p-12 <= tenth ? 3 : res * 0x1p-18 <= tenth ? 4 : 0;
       int used = 0;
       {
-        AccurateScope scope(c, 2, true);
+        AccurateScope scope(c, 2, slices);
         response_mo_fp64(c, dlt, nset, adl, true);
         used = scope.used;
       }

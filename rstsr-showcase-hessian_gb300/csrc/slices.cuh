@@ -17,15 +17,20 @@ struct Exact6 {
   static constexpr bool BF16 = true;
   using Elem = __nv_bfloat16;
 };
-// The same exact BF16 slice planes read in correction precision: only slices 0-3 of each
-// operand and the 10 products with t + u <= 3 (dropped terms ~2^-24 relative to the row and
-// column maxima), for operators applied to a small correction whose result only has to be
-// accurate relative to the correction itself.  Same planes, same exact accumulation bounds.
-struct Exact6c {
-  static constexpr int S = 4, NACC = 4, EOFF = 0, STAGES = 3;
+// The same exact BF16 slice planes read in correction precision: only slices 0 .. NS-1 of each
+// operand and the products with t + u <= NS - 1, for operators applied to a small correction
+// whose result only has to be accurate relative to the correction itself.  NS = 4: 10
+// products, each operand cut at 2^-25 of its row / column maximum, dropped products below
+// 2^-23 of the maxima's product; NS = 3: 6 products, 2^-19 and 2^-17.  Same planes, same exact
+// accumulation bounds; with NS = 3 the fourth accumulator stays unused.
+template <int NS>
+struct ExactC {
+  static constexpr int S = NS, NACC = 4, EOFF = 0, STAGES = 3;
   static constexpr bool BF16 = true;
   using Elem = __nv_bfloat16;
 };
+using Exact6c = ExactC<4>;
+using Exact6c3 = ExactC<3>;
 struct Split2 {
   static constexpr int S = 2, NACC = 1, EOFF = 14, STAGES = 6;
   static constexpr bool BF16 = false;
@@ -117,6 +122,23 @@ __device__ __forceinline__ void slice6(float2 x, int e, __nv_bfloat16* dst, int6
   }
 }
 
+// The same digits of an FP32 pair already scaled by 2^(36 - e) (x f1 f2, f1 f2 = 2^(36 - e)
+// as two normal powers of two, so that no ldexpf is needed), into d[0 .. NS).
+template <int NS>
+__device__ __forceinline__ void digits_pair(float hi, float lo, float f1, float f2, float* d) {
+  const bool bad = !isfinite(hi) || !isfinite(lo);
+  float r = (hi * f1) * f2;
+  const float l = (lo * f1) * f2;
+#pragma unroll
+  for (int t = 0; t < NS; ++t) {
+    if (t == 3) r += l;
+    const int sh = 30 - 6 * t;
+    const float q = rintf(r * __int_as_float((127 - sh) << 23));  // r 2^-sh
+    r = fmaf(-q, __int_as_float((127 + sh) << 23), r);
+    d[t] = bad ? __int_as_float(0x7FC00000) : q * __int_as_float((127 - 6 * (t + 1)) << 23);
+  }
+}
+
 // store one element's planes: exact BF16 slices, or split FP16 hi/lo of x 2^(14 - e)
 template <class PR>
 struct Put;
@@ -125,9 +147,9 @@ struct Put<Exact6> {
   template <class T>
   __device__ static void put(T x, int e, __nv_bfloat16* dst, int64_t plane) { slice6(x, e, dst, plane); }
 };
-template <>
-struct Put<Exact6c> {  // only the four planes a correction-precision product reads
-  __device__ static void put(float2 x, int e, __nv_bfloat16* dst, int64_t plane) { slice6<4>(x, e, dst, plane); }
+template <int NS>
+struct Put<ExactC<NS>> {  // only the planes a correction-precision product reads
+  __device__ static void put(float2 x, int e, __nv_bfloat16* dst, int64_t plane) { slice6<NS>(x, e, dst, plane); }
 };
 template <>
 struct Put<Split2> {

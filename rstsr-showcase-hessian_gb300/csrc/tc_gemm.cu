@@ -175,6 +175,219 @@ __global__ void __launch_bounds__(128, 1)
   }
 }
 
+// ---- W generation: one persistent split-FP16 GEMM per aux chunk ---------------------------
+//   W_P[(j,a), i] = sum_nu bra[nu, j, a] Z_P[nu, i]   (term 2's cderi_oxo_1, src/ri_jk/hess_r.rs:172-176,
+//   with Z_P = B_P C_occ: mocc^T (B_P bra) reassociated as bra^T Z_P)
+// for all P of the chunk as one GEMM: rows m = j + nocc a (A = bra's planes, K = nu), columns
+// n = i + nocc Pl (B = Z's planes, whose rows (i, P) are contiguous), written as FP16 hi / lo
+// planes of W * wscale (one power of two per chunk, from an upper bound of |W|) straight
+// into the layout term 2 reads, out[j + ldj i + s_a a + s_p Pl] (K = j).
+//   warp 0 lane 0 -- TMA producer over the CTA's tiles, 2-stage ring of the four planes;
+//   warp 1        -- TMEM owner (2 x 256 columns); lane 0 issues the MMAs of tile t into
+//                    accumulator t & 1 while the epilogue drains the other;
+//   warps 2-9     -- epilogue: TMEM lane quarter warp & 3, column half (warp - 2) / 4.
+// Tiles in a grouped raster: group_m row tiles walk every column tile with rows fastest, so a
+// group's A tiles stay in L2 while B streams once per group.
+struct WgArgs {
+  __half* out_hi;
+  __half* out_lo;
+  int M, N;            // rows (nocc nb), columns (nocc npc)
+  int nkb;             // K blocks of 64 (nu)
+  int m_tiles, n_tiles, group_m;
+  int b_row0;          // B row of column 0 (nocc P0)
+  int no;              // j = m % no, a = m / no; i = n % no, Pl = n / no
+  int ldj, s_a, s_p;   // 32-bit element offsets (the host checks the plane size)
+  const int* e_row;    // exponent of A row m's planes (the product carries 2^(e_row + e_col - 2 EOFF))
+  const int* e_col;    // exponent of B row b_row0 + n
+  const float* wscale; // power of two
+  int* err;
+};
+constexpr int WG_THREADS = 320, WG_EPI_WARPS = 8, WG_ACC = 256;
+constexpr int SPLIT_EOFF = 14;  // FP16 planes: x 2^(14 - e), e the exponent of the row's max
+
+__device__ __forceinline__ void wg_tile(const WgArgs& a, int t, int& m0, int& n0) {
+  const int per_group = a.group_m * a.n_tiles;
+  const int g = t / per_group, r = t % per_group;
+  const int gm0 = g * a.group_m;
+  const int gm = min(a.group_m, a.m_tiles - gm0);
+  m0 = (gm0 + r % gm) * BM;
+  n0 = (r / gm) * BN;
+}
+
+__global__ void __launch_bounds__(WG_THREADS, 1)
+    tc_wgen_kernel(const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
+                   const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl, WgArgs args) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5);
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES);
+  const uint32_t accf0 = smem_u32(bars + 2 * STAGES), acce0 = smem_u32(bars + 2 * STAGES + 2);
+  const uint32_t done = smem_u32(bars + 2 * STAGES + 4);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tiles = args.m_tiles * args.n_tiles;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(accf0 + 8 * b, 1);
+      mbar_init(acce0 + 8 * b, WG_EPI_WARPS);
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) tmem_alloc(smem_u32(tmem_slot), 2 * WG_ACC);
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    int it = 0, issued = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+      int m0, n0;
+      wg_tile(args, t, m0, n0);
+      for (int kb = 0; kb < args.nkb; ++kb, ++it) {
+        const int s = it % STAGES;
+        if (!mbar_wait(empty0 + 8 * s, ((it / STAGES) & 1) ^ 1, args.err)) { ok = false; break; }
+        issued = it + 1;
+        const uint32_t full = full0 + 8 * s;
+        mbar_expect_tx(full, STAGE_BYTES);
+        const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+        tma_load_3d(st, &mAh, full, kb * BK, m0, 0);
+        tma_load_3d(st + A_TILE, &mAl, full, kb * BK, m0, 0);
+        tma_load_3d(st + 2 * A_TILE, &mBh, full, kb * BK, args.b_row0 + n0, 0);
+        tma_load_3d(st + 2 * A_TILE + B_TILE, &mBl, full, kb * BK, args.b_row0 + n0, 0);
+      }
+    }
+    // the copies of the last round of every stage have landed before the CTA may exit
+    for (int i = max(0, issued - STAGES); i < issued; ++i) mbar_wait(full0 + 8 * (i % STAGES), (i / STAGES) & 1, nullptr);
+  } else if (warp == 1 && lane == 0) {
+    constexpr uint32_t idesc = instr_desc_f16(BM, BN, false);
+    int it = 0, lt = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++lt) {
+      const int b = lt & 1;
+      if (!mbar_wait(acce0 + 8 * b, ((lt >> 1) & 1) ^ 1, args.err)) break;
+      fence_after_sync();
+      const uint32_t acc = tmem + (uint32_t)(b * WG_ACC);
+      for (int kb = 0; kb < args.nkb; ++kb, ++it) {
+        const int s = it % STAGES;
+        if (!mbar_wait(full0 + 8 * s, (it / STAGES) & 1, args.err)) { ok = false; break; }
+        fence_after_sync();
+        const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+        const uint64_t ah = smem_desc<128>(st), al = smem_desc<128>(st + A_TILE);
+        const uint64_t bh = smem_desc<128>(st + 2 * A_TILE), bl = smem_desc<128>(st + 2 * A_TILE + B_TILE);
+#pragma unroll
+        for (int k = 0; k < BK / 16; ++k) {
+          const uint64_t dk = (uint64_t)((k * 32) >> 4);
+          mma_f16(acc, ah + dk, bh + dk, idesc, (kb > 0 || k > 0) ? 1u : 0u);
+          mma_f16(acc, ah + dk, bl + dk, idesc, 1u);
+          mma_f16(acc, al + dk, bh + dk, idesc, 1u);
+        }
+        mma_commit(empty0 + 8 * s);
+      }
+      if (ok) mma_commit(accf0 + 8 * b);
+    }
+    // every issued MMA has retired before TMEM is released (also after an early exit)
+    mma_commit(done);
+    mbar_wait(done, 0, nullptr);
+  } else if (warp >= 2) {
+    const int q = warp & 3, h = (warp - 2) >> 2;
+    // W's scale is a power of two: its exponent joins the row's and the column's
+    const int ews = (int)((__float_as_uint(*args.wscale) >> 23) & 0xFF) - 127;
+    // per tile: the row's exponent and the exponents of the lane's four columns, fetched one
+    // tile ahead so that their load latency overlaps the previous tile's epilogue
+    int m0n = 0, n0n = 0, erow_n = 0, ecl_n[4] = {0, 0, 0, 0};
+    auto fetch = [&](int tt) {
+      if (tt >= tiles) return;
+      wg_tile(args, tt, m0n, n0n);
+      const int m = m0n + q * 32 + lane;
+      erow_n = m < args.M ? args.e_row[m] : 0;
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) {
+        const int nl = n0n + h * 128 + cc * 32 + lane;
+        ecl_n[cc] = nl < args.N ? args.e_col[args.b_row0 + nl] : 0;
+      }
+    };
+    fetch(blockIdx.x);
+    int lt = 0;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++lt) {
+      const int b = lt & 1;
+      const int m0 = m0n, n0 = n0n;
+      int ecl[4];
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) ecl[cc] = ecl_n[cc];
+      const int m = m0 + q * 32 + lane;
+      const bool row_ok = m < args.M;
+      // the exponent of row m with the planes' offsets and W's scale (biased by 127)
+      const int erow = erow_n - 2 * SPLIT_EOFF + ews + 127;
+      fetch(t + gridDim.x);
+      // warp-uniform decision: tcgen05.ld is a whole-warp instruction
+      if (!__all_sync(0xffffffffu, mbar_wait(accf0 + 8 * b, (lt >> 1) & 1, args.err))) break;
+      fence_after_sync();
+      const int roff = row_ok ? (m % args.no) + (m / args.no) * args.s_a : 0;
+      const bool rows_ok = __all_sync(0xffffffffu, row_ok);
+#pragma unroll 1
+      for (int cc = 0; cc < 4; ++cc) {
+        const int c0 = n0 + h * 128 + cc * 32;
+        float v[32];
+        tmem_ld32(tmem + (uint32_t)(b * WG_ACC) + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * 128 + cc * 32), v);
+        // this lane's column: exponent and output offset, broadcast by shuffles
+        const int nl = c0 + lane;
+        const int ec = cc == 0 ? ecl[0] : cc == 1 ? ecl[1] : cc == 2 ? ecl[2] : ecl[3];  // registers, not local memory
+        const int col = nl < args.N ? (nl % args.no) * args.ldj + (nl / args.no) * args.s_p : 0;
+        const int jn = min(32, args.N - c0);
+        // the factor 2^(e) with e = erow + ec - 127 as a bit pattern when it is a normal float
+        // for the whole chunk (the common case), else clamped to the normal range: a nonzero
+        // |v| >= 2^-48 (sums of FP16 products) with |v 2^e| <= 2^14 (the bound) keeps e <= 62,
+        // and below 2^-126 v 2^e is under FP16's smallest subnormal either way, so the clamp
+        // changes no stored plane
+        int emn = ec, emx = ec;
+        for (int o = 16; o > 0; o >>= 1) {
+          emn = min(emn, __shfl_xor_sync(0xffffffffu, emn, o));
+          emx = max(emx, __shfl_xor_sync(0xffffffffu, emx, o));
+        }
+        const bool fast = rows_ok && jn == 32 && __all_sync(0xffffffffu, erow + emn >= 1 && erow + emx <= 254);
+        if (fast) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int off = roff + __shfl_sync(0xffffffffu, col, j);
+            const float x = v[j] * __uint_as_float((unsigned)(erow + __shfl_sync(0xffffffffu, ec, j)) << 23);
+            const __half hh = __float2half_rn(x);
+            __stcs(args.out_hi + off, hh);
+            __stcs(args.out_lo + off, __float2half_rn(x - __half2float(hh)));
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int ecj = __shfl_sync(0xffffffffu, ec, j);
+            const int co = __shfl_sync(0xffffffffu, col, j);
+            if (row_ok && j < jn) {
+              const int e = min(max(erow + ecj, 1), 254);
+              const float x = v[j] * __uint_as_float((unsigned)e << 23);
+              const __half hh = __float2half_rn(x);
+              __stcs(args.out_hi + (roff + co), hh);
+              __stcs(args.out_lo + (roff + co), __float2half_rn(x - __half2float(hh)));
+            }
+          }
+        }
+      }
+      fence_before_sync();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acce0 + 8 * b);
+    }
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  if (warp == 1) tmem_dealloc(tmem, 2 * WG_ACC);
+}
+
 // ---- FP16 plane splitting --------------------------------------------------------------
 __device__ __forceinline__ void split_f16(double x, double s, __half* hi, __half* lo) {
   const double xs = x * s;
@@ -273,7 +486,8 @@ bool tc_available(cphf_ctx* c) {
   if (major != 10 || encode_fn() == nullptr) return false;
   static bool attr_set = false;
   if (!attr_set) {
-    if (cudaFuncSetAttribute(tc_term1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess) {
+    if (cudaFuncSetAttribute(tc_term1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess ||
+        cudaFuncSetAttribute(tc_wgen_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES) != cudaSuccess) {
       cudaGetLastError();
       return false;
     }
@@ -364,7 +578,8 @@ void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, 
 
 void tc_planes_term(cphf_ctx* c, const __half* a_hi, const __half* a_lo, int64_t a_depth, int64_t a_off,
                     const __half* b_hi, const __half* b_lo, int64_t npc, int64_t M, int64_t N, int64_t K, int64_t ld,
-                    const double* rowscale, const double* colscale, float* out, int64_t ld_out, int* err) {
+                    const double* rowscale, const double* colscale, float* out, int64_t ld_out, int* err,
+                    const float* scale) {
   if (M <= 0 || N <= 0 || K <= 0 || npc <= 0) return;
   const int m_tiles = (int)div_up(M, BM), n_tiles = (int)div_up(N, BN);
   const CUtensorMap mAh = make_map(a_hi, K, M, a_depth, ld, BM);
@@ -384,12 +599,49 @@ void tc_planes_term(cphf_ctx* c, const __half* a_hi, const __half* a_lo, int64_t
   a.p_per_cta = (int)div_up(npc, ranges);
   a.pA0 = (int)a_off;
   a.m_tiles = m_tiles;
-  a.scale = nullptr;
+  a.scale = scale;
   a.rowscale = rowscale;
   a.colscale = colscale;
   a.err = err;
   dim3 grid((unsigned)tiles, (unsigned)div_up(npc, a.p_per_cta));
   tc_term1_kernel<<<grid, 128, SMEM_BYTES, c->stream>>>(mAh, mAl, mBh, mBl, a);
+  count_launch();
+  CPHF_CUDA(cudaGetLastError());
+}
+
+void tc_wgen_planes(cphf_ctx* c, const __half* a_hi, const __half* a_lo, int64_t M, const __half* b_hi,
+                    const __half* b_lo, int64_t b_rows, int64_t b_row0, int64_t N, int64_t K, int64_t ldk,
+                    const int* e_row, const int* e_col, const float* wscale, int64_t no, int64_t ldj, int64_t s_a,
+                    int64_t s_p, __half* out_hi, __half* out_lo, int* err) {
+  if (M <= 0 || N <= 0 || K <= 0) return;
+  const int64_t last = (no - 1) + ldj * (no - 1) + s_a * ((M - 1) / no) + s_p * ((N - 1) / no);
+  if (last >= (int64_t)INT32_MAX || b_row0 + N > (int64_t)INT32_MAX)
+    throw Error(CPHF_ERR_ARG, "W generation: plane offsets exceed 32 bits");
+  WgArgs a;
+  a.out_hi = out_hi;
+  a.out_lo = out_lo;
+  a.M = (int)M;
+  a.N = (int)N;
+  a.nkb = (int)div_up(K, BK);
+  a.m_tiles = (int)div_up(M, BM);
+  a.n_tiles = (int)div_up(N, BN);
+  a.group_m = std::min(a.m_tiles, 32);
+  a.b_row0 = (int)b_row0;
+  a.no = (int)no;
+  a.ldj = (int)ldj;
+  a.s_a = (int)s_a;
+  a.s_p = (int)s_p;
+  a.e_row = e_row;
+  a.e_col = e_col;
+  a.wscale = wscale;
+  a.err = err;
+  const CUtensorMap mAh = make_map(a_hi, K, M, 1, ldk, BM);
+  const CUtensorMap mAl = make_map(a_lo, K, M, 1, ldk, BM);
+  const CUtensorMap mBh = make_map(b_hi, K, b_rows, 1, ldk, BN);
+  const CUtensorMap mBl = make_map(b_lo, K, b_rows, 1, ldk, BN);
+  const int64_t tiles = (int64_t)a.m_tiles * a.n_tiles;
+  const unsigned grid = (unsigned)std::min<int64_t>(tiles, c->num_sms);
+  tc_wgen_kernel<<<grid, WG_THREADS, SMEM_BYTES, c->stream>>>(mAh, mAl, mBh, mBl, a);
   count_launch();
   CPHF_CUDA(cudaGetLastError());
 }

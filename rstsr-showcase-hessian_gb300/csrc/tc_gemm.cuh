@@ -27,10 +27,21 @@ void tc_k_term1(cphf_ctx* c, const DevBuf& Bhi, const DevBuf& Blo, int64_t ldk, 
                 float* out, DevBuf& Thi, DevBuf& Tlo, const TPlanes& tplanes);
 // out[m + ld_out n] += rowscale[m] colscale[n] sum_{Pl < npc} sum_{k < K} A_(a_off+Pl)[m, k] B_Pl[n, k]
 // over split-FP16 planes (hi / lo, three products) with the term-1 kernel's 256-wide tiles:
-// A planes [a_depth][M][ld] per plane array, B planes [npc][N][ld]; FP32 atomics into out.
+// A planes [a_depth][M][ld] per plane array, B planes [npc][N][ld]; FP32 atomics into out;
+// `scale` (device, nullable) multiplies every element.
 void tc_planes_term(cphf_ctx* c, const __half* a_hi, const __half* a_lo, int64_t a_depth, int64_t a_off,
                     const __half* b_hi, const __half* b_lo, int64_t npc, int64_t M, int64_t N, int64_t K, int64_t ld,
-                    const double* rowscale, const double* colscale, float* out, int64_t ld_out, int* err);
+                    const double* rowscale, const double* colscale, float* out, int64_t ld_out, int* err,
+                    const float* scale = nullptr);
+// W generation as one GEMM over a chunk of aux functions: rows m = j + no a of A (bra's FP16
+// planes, K-major, [M][ldk]), columns n = i + no Pl from B rows b_row0 + n (Z's planes, rows
+// (i, P)); writes the FP16 hi / lo planes of W * (*wscale) (a power of two) to
+// out[j + ldj i + s_a a + s_p Pl], with 2^(e_row[m] + e_col[b_row0 + n] - 28) undoing the
+// operands' plane scales.  Offsets must fit 32 bits.
+void tc_wgen_planes(cphf_ctx* c, const __half* a_hi, const __half* a_lo, int64_t M, const __half* b_hi,
+                    const __half* b_lo, int64_t b_rows, int64_t b_row0, int64_t N, int64_t K, int64_t ldk,
+                    const int* e_row, const int* e_col, const float* wscale, int64_t no, int64_t ldj, int64_t s_a,
+                    int64_t s_p, __half* out_hi, __half* out_lo, int* err);
 // scale[0] = 2^(14 - e) for max |T| = *mx < 2^e, scale[1] = alpha / (sA scale[0])
 void launch_t_scale(const unsigned* mx, float sA, float alpha, float* scale, cudaStream_t stream);
 

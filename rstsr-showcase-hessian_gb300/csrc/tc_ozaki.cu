@@ -107,7 +107,8 @@ struct OzArgs {
   const double* colscale;
   int64_t ld_out;
   // batched mode epilogue: out [(m % m_div) s_m1 + (m / m_div) s_m2 + n s_n + Pl s_p]
-  //   = 2^(e_row[m] + e_col[(b_off + Pl) N + n] - 2 EOFF) value (float2 pair: Exact6, float: Split2)
+  //   = 2^(e_row[m] + e_col[(b_off + Pl) N + n] - 2 EOFF) value (float2 pair: Exact6, float: Split2;
+  //   EPI_SPLIT16 takes e_col uniform over an aux function's columns and reads its first)
   const int* e_row;
   const int* e_col;
   int64_t m_div, s_m1, s_m2, s_n, s_p;
@@ -257,7 +258,12 @@ __global__ void __launch_bounds__(128, 1)
           tmem_ld32(lane_base + (uint32_t)(0 * BN + c * 32), v0);
           tmem_ld32(lane_base + (uint32_t)(1 * BN + c * 32), v1);
           tmem_ld32(lane_base + (uint32_t)(2 * BN + c * 32), v2);
-          tmem_ld32(lane_base + (uint32_t)(3 * BN + c * 32), v3);
+          if constexpr (PR::S > 3) {
+            tmem_ld32(lane_base + (uint32_t)(3 * BN + c * 32), v3);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) v3[j] = 0.f;  // groups 0-2 only: the fourth accumulator is unused
+          }
           if (row_ok) {
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
@@ -350,10 +356,42 @@ struct Batched {
   static constexpr int SMEM_BYTES = STAGES * Cfg<PR, BN>::STAGE_BYTES + 1024 + 1024;
 };
 
-// 2^e as a float (exact); ldexpf outside the normal range
+// 2^e as a float for any int e, exact: normal, subnormal below 2^-126, 0 below 2^-149, inf
+// above 2^127 (branch-free integer arithmetic on the bit pattern)
 __device__ __forceinline__ float pow2f(int e) {
-  return (e >= -126 && e <= 127) ? __int_as_float((e + 127) << 23) : ldexpf(1.f, e);
+  const int c = min(max(e, -150), 128);
+  const unsigned normal = (unsigned)(c + 127) << 23;                 // c in [-126, 128]
+  const unsigned sub = c >= -149 ? 1u << ((c + 149) & 31) : 0u;      // c in [-149, -127]
+  return __uint_as_float(c >= -126 ? normal : sub);
 }
+
+// FP16 hi / lo planes of v[j] f to ph[j sn], pl[j sn] for j < jn, as streaming (evict-first)
+// stores: T is read once, by term 1, after its chunk is complete.  A full chunk (jn = 32, the
+// warp-uniform common case) runs without per-element predicates.
+__device__ __forceinline__ void store_split32(const float* v, float f, __half* ph, __half* pl, int sn, int jn) {
+  if (jn >= 32) {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const float x = v[j] * f;
+      const __half h = __float2half_rn(x);
+      __stcs(ph + j * sn, h);
+      __stcs(pl + j * sn, __float2half_rn(x - __half2float(h)));
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      if (j < jn) {
+        const float x = v[j] * f;
+        const __half h = __float2half_rn(x);
+        __stcs(ph + j * sn, h);
+        __stcs(pl + j * sn, __float2half_rn(x - __half2float(h)));
+      }
+    }
+  }
+}
+
+// exponent of a power-of-two float (normal or inf)
+__device__ __forceinline__ int pow2_exponent(float s) { return (int)((__float_as_uint(s) >> 23) & 0xFF) - 127; }
 
 // EPI: store the scaled values (T / W staging) or FP16 hi / lo planes of them times *tscale.
 // EPI_STOREMAX (exact slices): store as EPI_STORE and reduce max |value| per staging column
@@ -491,51 +529,88 @@ __global__ void __launch_bounds__(320, PR::NACC == 4 ? 1 : 2)
 #pragma unroll
         for (int j = 0; j < 32; ++j) cmax[j] = 0.f;
       }
+      // the column exponent of aux function p + 1 is fetched while p is processed (its load
+      // latency would otherwise stall every aux function's epilogue)
+      const int* const ecp = args.e_col + (int64_t)(args.b_off + p_begin) * args.N + ncol;
+      int ec_next = (nP > 0 && ncol < args.N) ? ecp[0] : 0;
       for (int p = 0; p < nP; ++p) {
         const int b = p & 1;
+        const int ec = ec_next;
+        if (p + 1 < nP && ncol < args.N) ec_next = ecp[(int64_t)(p + 1) * args.N];
         // warp-uniform decision: tcgen05.ld is a whole-warp instruction
         if (!__all_sync(0xffffffffu, mbar_wait(accf0 + 8 * b, (p >> 1) & 1, args.err))) break;
         fence_after_sync();
         const int Pl = p_begin + p;
         const uint32_t lane_base = tmem + (uint32_t)b * ACC + ((uint32_t)(q * 32) << 16);
-        const int ec = ncol < args.N ? args.e_col[(int64_t)(args.b_off + Pl) * args.N + ncol] : 0;
         const int64_t pbase = base + (int64_t)Pl * args.s_p;
         if constexpr (PR::NACC == 4) {
-          float v0[32], v1[32], v2[32], v3[32];
-          tmem_ld32(lane_base + (uint32_t)(0 * BN + c * 32), v0);
-          tmem_ld32(lane_base + (uint32_t)(1 * BN + c * 32), v1);
-          tmem_ld32(lane_base + (uint32_t)(2 * BN + c * 32), v2);
-          tmem_ld32(lane_base + (uint32_t)(3 * BN + c * 32), v3);
+          float2* const o = reinterpret_cast<float2*>(args.out) + pbase + (int64_t)(n0 + c * 32) * args.s_n;
+          const int sn = (int)args.s_n;
+          // the common case without per-element predicates or range checks: every row and
+          // column of the chunk in range, every factor 2^(erow + ec) a normal float (its bit
+          // pattern (erow + ec + 127) << 23)
+          int emn = ec, emx = ec;
+          for (int o2 = 16; o2 > 0; o2 >>= 1) {
+            emn = min(emn, __shfl_xor_sync(0xffffffffu, emn, o2));
+            emx = max(emx, __shfl_xor_sync(0xffffffffu, emx, o2));
+          }
+          const bool fast = __all_sync(0xffffffffu, row_ok && erow + emn >= -126 && erow + emx <= 127) &&
+                            args.N - (n0 + c * 32) >= 32;
+          const int eb = erow + 127;
+          // two halves of 16 columns: four accumulators of 16 columns in registers at a time
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int n = n0 + c * 32 + j;
-            const float f = pow2f(erow + __shfl_sync(0xffffffffu, ec, j));
-            if (row_ok && n < args.N) {
-              float hi, lo;
-              combine4(v0[j], v1[j], v2[j], v3[j], hi, lo);
-              reinterpret_cast<float2*>(args.out)[pbase + n * args.s_n] = make_float2(hi * f, lo * f);
-              if constexpr (EPI == EPI_STOREMAX) cmax[j] = fmaxf(cmax[j], fabsf(hi * f));
+          for (int hf = 0; hf < 2; ++hf) {
+            float v0[16], v1[16], v2[16], v3[16];
+            tmem_ld16x4(lane_base + (uint32_t)(0 * BN + c * 32 + 16 * hf), lane_base + (uint32_t)(1 * BN + c * 32 + 16 * hf),
+                        lane_base + (uint32_t)(2 * BN + c * 32 + 16 * hf), lane_base + (uint32_t)(3 * BN + c * 32 + 16 * hf),
+                        v0, v1, v2, v3);
+            if constexpr (PR::S <= 3) {
+#pragma unroll
+              for (int jj = 0; jj < 16; ++jj) v3[jj] = 0.f;  // groups 0-2 only: the fourth accumulator is unused
+            }
+            if (fast) {
+#pragma unroll
+              for (int jj = 0; jj < 16; ++jj) {
+                const int j = 16 * hf + jj;
+                const float f = __uint_as_float((unsigned)(eb + __shfl_sync(0xffffffffu, ec, j)) << 23);
+                float hi, lo;
+                combine4(v0[jj], v1[jj], v2[jj], v3[jj], hi, lo);
+                __stcs(o + j * sn, make_float2(hi * f, lo * f));
+                if constexpr (EPI == EPI_STOREMAX) cmax[j] = fmaxf(cmax[j], fabsf(hi * f));
+              }
+            } else {
+#pragma unroll
+              for (int jj = 0; jj < 16; ++jj) {
+                const int j = 16 * hf + jj;
+                const float f = pow2f(erow + __shfl_sync(0xffffffffu, ec, j));
+                if (row_ok && n0 + c * 32 + j < args.N) {
+                  float hi, lo;
+                  combine4(v0[jj], v1[jj], v2[jj], v3[jj], hi, lo);
+                  __stcs(o + j * sn, make_float2(hi * f, lo * f));
+                  if constexpr (EPI == EPI_STOREMAX) cmax[j] = fmaxf(cmax[j], fabsf(hi * f));
+                }
+              }
             }
           }
+        } else if constexpr (EPI == EPI_SPLIT16) {
+          // B (O_P) carries one exponent per aux function: one factor per row and P, with
+          // T's power-of-two scale folded into the exponent
+          float v[32];
+          tmem_ld32(lane_base + (uint32_t)(c * 32), v);
+          // (every column of O_P carries the aux function's exponent: lane 0's, fetched ahead)
+          const float f = pow2f(erow + __shfl_sync(0xffffffffu, ec, 0) + pow2_exponent(*args.tscale));
+          const int64_t off = pbase + (int64_t)(n0 + c * 32) * args.s_n;
+          if (row_ok)
+            store_split32(v, f, reinterpret_cast<__half*>(args.out) + off, reinterpret_cast<__half*>(args.out_lo) + off,
+                          (int)args.s_n, min(32, args.N - (n0 + c * 32)));
         } else {
           float v[32];
           tmem_ld32(lane_base + (uint32_t)(c * 32), v);
-          const float ts = EPI == EPI_SPLIT16 ? *args.tscale : 1.f;
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             const int n = n0 + c * 32 + j;
             const float f = pow2f(erow + __shfl_sync(0xffffffffu, ec, j));
-            if (row_ok && n < args.N) {
-              if constexpr (EPI == EPI_STORE) {
-                reinterpret_cast<float*>(args.out)[pbase + n * args.s_n] = v[j] * f;
-              } else {
-                const float x = (v[j] * f) * ts;
-                const __half h = __float2half_rn(x);
-                const int64_t off = pbase + n * args.s_n;
-                reinterpret_cast<__half*>(args.out)[off] = h;
-                reinterpret_cast<__half*>(args.out_lo)[off] = __float2half_rn(x - __half2float(h));
-              }
-            }
+            if (row_ok && n < args.N) __stcs(reinterpret_cast<float*>(args.out) + pbase + n * args.s_n, v[j] * f);
           }
         }
         fence_before_sync();
@@ -568,24 +643,44 @@ __global__ void __launch_bounds__(320, PR::NACC == 4 ? 1 : 2)
   if (warp == 1) tmem_dealloc(tmem, 2 * ACC);
 }
 
-// Inner T generation with the bra tile resident (split FP16, K = nocc <= 128): one CTA per
-// (row tile of (nu, a), range of aux functions).  The A tile -- every K block of the bra
-// rows, both planes -- is loaded once and stays in shared memory; only O_P's 128-row tile
-// (all i of a column, N = 128 >= nocc) streams through a 2-stage ring (98 KB in all, two CTAs
-// per SM).  Double-buffered TMEM accumulators (2 x 128 columns) let the epilogue of aux
-// function p (FP16 hi / lo planes of T * tscale, 8 warps of 64 columns each) overlap the MMAs
-// of p + 1.  Warp 0: TMA producer, warp 1: MMA issuer and TMEM owner, warps 2-9: epilogue.
+// Inner T generation with the bra tile resident (split FP16, K = nocc <= 128): one CTA per SM
+// and (row tile, range of aux functions).  A row tile is 128 consecutive nu of one perturbation
+// a (the last tile of each a is partial), so that T_P's tile is one box of the planes' layout.
+// The A tile -- every K block of the bra rows, both planes -- is loaded once and stays in
+// shared memory; O_P's 128-row tile (all i of a column, N = 128 >= nocc) streams through a
+// 4-stage ring.  Double-buffered TMEM accumulators (2 x 128 columns) let the epilogue of aux
+// function p overlap the MMAs of p + 1.  Each epilogue warp (32 nu x 64 i) writes the FP16
+// hi / lo planes of T * tscale of its part into its own shared-memory tile [64 i][32 nu] and
+// stores them with TMA (cp.async.bulk.tensor, clipped at nu = nao): the global writes are bulk
+// transfers off the warps' issue path, and a warp waits only for its own previous stores to
+// have left shared memory, so the stores of aux function p drain while p + 1 is computed.
+// Warp 0: TMA loads, warp 1: MMA issuer and TMEM owner, warps 2-9: epilogue.
 struct ResT {
-  static constexpr int BN = 128, STAGES = 2, MAX_KB = 4, THREADS = 320, EPI_WARPS = 8;
+  static constexpr int BN = 128, STAGES = 4, MAX_KB = 4, THREADS = 320, EPI_WARPS = 8;
   static constexpr int A_TILE = BM * BK * 2;            // 8 KB: one K block of one plane
   static constexpr int B_TILE = BN * BK * 2;            // 8 KB
   static constexpr int A_BYTES = MAX_KB * 2 * A_TILE;   // 64 KB resident
   static constexpr int STAGE_BYTES = 2 * B_TILE;        // hi + lo of one K block of O_P
-  static constexpr int SMEM_BYTES = A_BYTES + STAGES * STAGE_BYTES + 1024 + 1024;
+  static constexpr int WARP_OUT = 2 * 64 * 32 * 2;     // one warp's staged hi + lo tiles: 64 i x 32 nu
+  static constexpr int OUT_BYTES = EPI_WARPS * WARP_OUT;
+  static constexpr int SMEM_BYTES = A_BYTES + STAGES * STAGE_BYTES + OUT_BYTES + 1024 + 1024;
 };
 
-__global__ void __launch_bounds__(320, 2)
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, uint32_t src, int c0, int c1, int c2) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(src), "r"(c0), "r"(c1), "r"(c2)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+__global__ void __launch_bounds__(320, 1)
     tc_tgen_resident_kernel(const __grid_constant__ CUtensorMap mA, const __grid_constant__ CUtensorMap mB,
+                            const __grid_constant__ CUtensorMap mTh0, const __grid_constant__ CUtensorMap mTh1,
+                            const __grid_constant__ CUtensorMap mTl0, const __grid_constant__ CUtensorMap mTl1,
                             OzArgs args) {
   constexpr int STAGES = ResT::STAGES, BN = ResT::BN;
   constexpr uint32_t ACC = BN;
@@ -593,17 +688,23 @@ __global__ void __launch_bounds__(320, 2)
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* ares = smem;
   uint8_t* ring = smem + ResT::A_BYTES;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(ring + STAGES * ResT::STAGE_BYTES);
+  uint8_t* outs = ring + STAGES * ResT::STAGE_BYTES;  // per epilogue warp: [plane][64 i][32 nu] FP16
+  uint64_t* bars = reinterpret_cast<uint64_t*>(outs + ResT::OUT_BYTES);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 6);
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + STAGES);
   const uint32_t accf0 = smem_u32(bars + 2 * STAGES), acce0 = smem_u32(bars + 2 * STAGES + 2);
   const uint32_t done = smem_u32(bars + 2 * STAGES + 4), abar = smem_u32(bars + 2 * STAGES + 5);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * BM;
+  // row tile: 128 nu of perturbation a (rows a nao + nu of the bra planes)
+  const int nao = (int)args.m_div;
+  const int tpa = (nao + BM - 1) / BM;
+  const int a_pert = blockIdx.y / tpa, nu0 = (blockIdx.y % tpa) * BM;
+  const int m0 = a_pert * nao + nu0;
   const int p_begin = blockIdx.x * args.p_per_cta;
   const int nP = min(args.np - p_begin, args.p_per_cta);
   const int nkb = args.nkb;  // <= MAX_KB (host checks)
+  const int no = args.N;     // <= BN (host checks)
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -678,48 +779,74 @@ __global__ void __launch_bounds__(320, 2)
       mma_commit(done);
       mbar_wait(done, 0, nullptr);
     } else if (warp >= 2) {
-      // epilogue: TMEM lane quarter q, columns [64 h, 64 h + 64)
+      // epilogue: TMEM lane quarter q (rows nu0 + 32 q + lane), columns i in [64 h, 64 h + ni)
       const int q = warp & 3;
       const int h = (warp - 2) >> 2;
-      const int row = m0 + q * 32 + lane;
-      const bool row_ok = row < args.M;
-      int erow = 0;
-      int64_t base = 0;
-      if (row_ok) {
-        erow = args.e_row[row] - 2 * Split2::EOFF;
-        base = (row % args.m_div) * args.s_m1 + (row / args.m_div) * args.s_m2;
-      }
+      const int ni = min(64, no - 64 * h);  // this warp's columns (none when nocc <= 64 and h = 1)
+      const int nul = q * 32 + lane;
+      const bool row_ok = nu0 + nul < nao;
+      const int erow = row_ok ? args.e_row[m0 + nul] - 2 * Split2::EOFF : 0;
+      // T's scale is a power of two: its exponent joins the row's and the aux function's
+      const int ets = pow2_exponent(*args.tscale);
+      // O_P's planes carry one exponent per aux function, so the row has one factor per P; the
+      // exponent of p + 1 is fetched while p is processed
+      const int* const eP = args.e_col + (int64_t)(args.b_off + p_begin) * args.N;
+      int e_next = eP[0];
+      uint8_t* const wst = outs + (warp - 2) * ResT::WARP_OUT;
+      __half* const sh = reinterpret_cast<__half*>(wst) + lane;  // [64 i][32 nu]
+      __half* const sl = sh + 64 * 32;
+      const CUtensorMap* const mh = h == 0 ? &mTh0 : &mTh1;
+      const CUtensorMap* const ml = h == 0 ? &mTl0 : &mTl1;
       for (int p = 0; p < nP; ++p) {
         const int b = p & 1;
+        const int e_p = e_next;
+        if (p + 1 < nP) e_next = eP[(int64_t)(p + 1) * args.N];
+        // this warp's staged tiles of p - 1 have left shared memory before they are overwritten
+        if (lane == 0) bulk_wait_read0();
+        __syncwarp();
         if (!__all_sync(0xffffffffu, mbar_wait(accf0 + 8 * b, (p >> 1) & 1, args.err))) break;
         fence_after_sync();
-        const int Pl = p_begin + p;
-        const int64_t pbase = base + (int64_t)Pl * args.s_p;
-        const float ts = *args.tscale;
+        float v[2][32];
+        const uint32_t tb = tmem + (uint32_t)b * ACC + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * 64);
+        tmem_ld32x2(tb, tb + 32, v[0], v[1]);
+        fence_before_sync();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(acce0 + 8 * b);  // accumulator b may take aux p + 2
+        if (ni <= 0) continue;
+        const float f = pow2f(erow + e_p + ets);
 #pragma unroll
         for (int cc = 0; cc < 2; ++cc) {
-          const int c0 = h * 64 + cc * 32;
-          float v[32];
-          tmem_ld32(tmem + (uint32_t)b * ACC + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
-          const int ncol = c0 + lane;
-          const int ec = ncol < args.N ? args.e_col[(int64_t)(args.b_off + Pl) * args.N + ncol] : 0;
+          const int jn = min(32, ni - 32 * cc);
+          if (jn >= 32) {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int n = c0 + j;
-            const float f = pow2f(erow + __shfl_sync(0xffffffffu, ec, j));
-            if (row_ok && n < args.N) {
-              const float x = (v[j] * f) * ts;
+            for (int j = 0; j < 32; ++j) {
+              const float x = v[cc][j] * f;
               const __half hh = __float2half_rn(x);
-              const int64_t off = pbase + n * args.s_n;
-              reinterpret_cast<__half*>(args.out)[off] = hh;
-              reinterpret_cast<__half*>(args.out_lo)[off] = __float2half_rn(x - __half2float(hh));
+              sh[(32 * cc + j) * 32] = hh;
+              sl[(32 * cc + j) * 32] = __float2half_rn(x - __half2float(hh));
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              if (j < jn) {
+                const float x = v[cc][j] * f;
+                const __half hh = __float2half_rn(x);
+                sh[(32 * cc + j) * 32] = hh;
+                sl[(32 * cc + j) * 32] = __float2half_rn(x - __half2float(hh));
+              }
             }
           }
         }
-        fence_before_sync();
+        fence_proxy_async();  // the generic-proxy writes are visible to the TMA stores
         __syncwarp();
-        if (lane == 0) mbar_arrive(acce0 + 8 * b);
+        if (lane == 0 && nu0 + 32 * q < nao) {  // (a box wholly past nu = nao has nothing to store)
+          const int Pl = p_begin + p;
+          tma_store_3d(mh, smem_u32(wst), nu0 + 32 * q, a_pert * no + 64 * h, Pl);
+          tma_store_3d(ml, smem_u32(wst + ResT::WARP_OUT / 2), nu0 + 32 * q, a_pert * no + 64 * h, Pl);
+          bulk_commit();
+        }
       }
+      if (lane == 0) bulk_wait0();  // the stores are complete before the CTA exits
     }
   }
   fence_before_sync();
@@ -746,6 +873,38 @@ __global__ void slice_rows_kernel(const TIn* __restrict__ src, int64_t rows, int
     const int e = key_exp(m, float_key<TIn>());
     for (int64_t k = lane; k < K; k += 32) Put<PR>::put(p[k * ks], e, dst + r * ld + k, plane);
     if (lane == 0) e_out[r] = e;
+  }
+}
+
+// Group slicer: rows [g rpg, (g + 1) rpg) of src (row r, element k at src[r K + k]) share one
+// exponent, that of the group's max; one block per group.  Planes to dst[t plane + r ld + k],
+// the exponent to e_out[r] for every row of the group.
+template <class PR, class TIn>
+__global__ void slice_groups_kernel(const TIn* __restrict__ src, int64_t groups, int64_t rpg, int64_t K,
+                                    typename PR::Elem* __restrict__ dst, int64_t ld, int64_t plane,
+                                    int* __restrict__ e_out) {
+  __shared__ unsigned long long red[32];
+  const int64_t n = rpg * K;
+  for (int64_t g = blockIdx.x; g < groups; g += gridDim.x) {
+    const TIn* p = src + g * n;
+    unsigned long long m = 0;
+    for (int64_t t = threadIdx.x; t < n; t += blockDim.x) m = max(m, abs_key(p[t]));
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0ull;
+      for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+      if (threadIdx.x == 0) red[0] = m;
+    }
+    __syncthreads();
+    const int e = key_exp(red[0], float_key<TIn>());
+    for (int64_t t = threadIdx.x; t < n; t += blockDim.x) {
+      const int64_t r = g * rpg + t / K, k = t % K;
+      Put<PR>::put(p[t], e, dst + r * ld + k, plane);
+    }
+    for (int64_t r = threadIdx.x; r < rpg; r += blockDim.x) e_out[g * rpg + r] = e;
+    __syncthreads();
   }
 }
 
@@ -796,31 +955,39 @@ __global__ void slice_zt_kernel(const TIn* __restrict__ Z, int64_t nao, int64_t 
   }
 }
 
-// max |x| of staging rows (Pl, n) of length K (row stride ld) per column n: one warp per row
-template <class TIn>
-__global__ void colmax_rows_kernel(const TIn* __restrict__ T, int64_t rows, int64_t N, int64_t ld, int64_t K,
-                                   unsigned long long* __restrict__ mx) {
+// Exact BF16 slices (the first NS planes) of FP32-pair staging rows: row r holds K pairs at
+// T[r ld + k] with the exponent of staging column r % N; planes [t][r][ld].  One warp per row,
+// two elements per lane and step (16-byte loads, BF16-pair stores), the scale 2^(36 - e) as two
+// exact power-of-two factors (e in [-149, 128] keeps both normal).
+template <int NS>
+__global__ void slice_pairs_kernel(const float2* __restrict__ T, int64_t rows, int64_t N, int64_t ld, int K,
+                                   const int* __restrict__ e_col, __nv_bfloat16* __restrict__ out) {
   const int lane = threadIdx.x & 31;
   const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t r = w0; r < rows; r += nw) {
-    unsigned long long m = 0;
-    for (int64_t k = lane; k < K; k += 32) m = max(m, abs_key(T[r * ld + k]));
-    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (lane == 0) atomicMax(mx + (r % N), m);
-  }
-}
-
-// planes [t][Pl][n][ld] of the staging T[Pl][n][k] with column exponent e_n, k < K
-template <class PR, class TIn>
-__global__ void slice_staging_kernel(const TIn* __restrict__ T, int64_t rows, int64_t N, int64_t ld, int64_t K,
-                                     const int* __restrict__ e_col, typename PR::Elem* __restrict__ out) {
-  const int64_t total = rows * K;
   const int64_t plane = rows * ld;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t k = t % K;
-    const int64_t r = t / K;
-    Put<PR>::put(T[r * ld + k], e_col[r % N], out + r * ld + k, plane);
+  for (int64_t r = w0; r < rows; r += nw) {
+    const int sc = 36 - e_col[r % N], s1 = sc >> 1, s2 = sc - s1;
+    const float f1 = __int_as_float((127 + s1) << 23), f2 = __int_as_float((127 + s2) << 23);
+    const float2* src = T + r * ld;
+    __nv_bfloat16* dst = out + r * ld;
+    for (int k = 2 * lane; k < K; k += 64) {
+      if (k + 1 < K) {
+        const float4 p = *reinterpret_cast<const float4*>(src + k);
+        float d0[NS], d1[NS];
+        digits_pair<NS>(p.x, p.y, f1, f2, d0);
+        digits_pair<NS>(p.z, p.w, f1, f2, d1);
+#pragma unroll
+        for (int t = 0; t < NS; ++t)
+          *reinterpret_cast<__nv_bfloat162*>(dst + t * plane + k) = __floats2bfloat162_rn(d0[t], d1[t]);
+      } else {
+        const float2 p = src[k];
+        float d0[NS];
+        digits_pair<NS>(p.x, p.y, f1, f2, d0);
+#pragma unroll
+        for (int t = 0; t < NS; ++t) dst[t * plane + k] = __float2bfloat16_rn(d0[t]);
+      }
+    }
   }
 }
 
@@ -852,6 +1019,23 @@ __global__ void bra_rowsum_max_kernel(const float* __restrict__ bra, int64_t nao
   }
   for (int o = 16; o > 0; o >>= 1) sum = fmaxf(sum, __shfl_xor_sync(0xffffffffu, sum, o));
   if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(sum));
+}
+
+// max over rows m of sum_k |x[k + K m]| (float bits, atomicMax into *out); one warp per row
+__global__ void rowsum_abs_max_kernel(const float* __restrict__ x, int64_t K, int64_t rows, unsigned* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  float best = 0.f;
+  for (int64_t r = w0; r < rows; r += nw) {
+    float sum = 0.f;
+    for (int64_t k = lane; k < K; k += 32) sum += fabsf(x[r * K + k]);
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    best = fmaxf(best, sum);
+  }
+  // rounding of the FP32 sums is covered by the FP16 planes' headroom (the bound maps to 2^14,
+  // FP16 holds 2^15)
+  if (lane == 0 && best > 0.f) atomicMax(out, __float_as_uint(best * 1.0001f));
 }
 
 // *mx = an upper bound of |T_P[nu, (i,a)]| = |sum_j bra[nu,j,a] O_P[j,i]| over P in [0, npc):
@@ -1074,33 +1258,57 @@ bool res_attr_ok() {
   return state == 1;
 }
 
-void launch_tgen_resident_raw(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, OzArgs a, int waves) {
-  const int64_t tiles = a.m_tiles;
+// row tiles: 128 nu of one perturbation (m_div = nao, M = nao nb)
+void launch_tgen_resident_raw(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, const CUtensorMap* mT,
+                              OzArgs a, int waves) {
+  const int64_t tiles = div_up(a.m_div, (int64_t)BM) * (a.M / a.m_div);
   if (tiles > 65535) throw Error(CPHF_ERR_ARG, "tensor-core T generation: grid too large");
   a.p_per_cta = (int)std::max<int64_t>(1, std::min<int64_t>(a.np, a.np * tiles / (waves * (int64_t)c->num_sms)));
   const dim3 grid((unsigned)div_up(a.np, a.p_per_cta), (unsigned)tiles);
-  tc_tgen_resident_kernel<<<grid, ResT::THREADS, ResT::SMEM_BYTES, c->stream>>>(mA, mB, a);
+  tc_tgen_resident_kernel<<<grid, ResT::THREADS, ResT::SMEM_BYTES, c->stream>>>(mA, mB, mT[0], mT[1], mT[2], mT[3],
+                                                                                 a);
   count_launch();
   CPHF_CUDA(cudaGetLastError());
 }
 
 // aux functions per CTA from the waves of CTAs over the SMs, tuned once per shape (every
 // candidate writes the same planes, so the last one's output stands)
-void launch_tgen_resident(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, const OzArgs& a) {
-  const TuneKey key{9000, a.M, a.N, a.nkb, a.np};
+void launch_tgen_resident(cphf_ctx* c, const CUtensorMap& mA, const CUtensorMap& mB, const CUtensorMap* mT,
+                          const OzArgs& a) {
+  const TuneKey key{9001, a.M, a.N, a.nkb, a.np};
   auto& tab = tune_table();
   int best = 2;
   if (!tab.find(key, best) && !capturing(c->stream)) {
     float best_ms = 0.f;
-    for (int w : {2, 4, 8}) {
-      const float ms = time_launch(c->stream, [&] { launch_tgen_resident_raw(c, mA, mB, a, w); });
+    for (int w : {1, 2, 4, 8}) {
+      const float ms = time_launch(c->stream, [&] { launch_tgen_resident_raw(c, mA, mB, mT, a, w); });
       if (best_ms == 0.f || ms < best_ms) best_ms = ms, best = w;
     }
     tab.put(key, best);
     return;
   }
-  launch_tgen_resident_raw(c, mA, mB, a, best);
+  launch_tgen_resident_raw(c, mA, mB, mT, a, best);
 }
+
+// 3-D FP16 map of T's planes for the TMA stores of the resident T generation: dims {nu (nao),
+// n = i + nocc a (N), Pl (npc)}, row stride ldt, box {32 nu, ni, 1} (one epilogue warp's part,
+// ni of its 64 columns), no swizzle (the staged tile is [ni][32] dense)
+CUtensorMap make_t_store_map(const __half* base, int64_t nao, int64_t N, int64_t npc, int64_t ldt, int64_t ni) {
+  CUtensorMap m;
+  std::memset(&m, 0, sizeof(m));
+  auto fn = encode_fn();
+  if (!fn) throw Error(CPHF_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  cuuint64_t dims[3] = {(cuuint64_t)nao, (cuuint64_t)N, (cuuint64_t)npc};
+  cuuint64_t strides[2] = {(cuuint64_t)(ldt * 2), (cuuint64_t)(ldt * 2 * N)};
+  cuuint32_t box[3] = {32, (cuuint32_t)ni, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 3, const_cast<__half*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw Error(CPHF_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  return m;
+}
+
 
 OzArgs base_args(OzState& z, int M, int N) {
   OzArgs a;
@@ -1122,7 +1330,8 @@ bool oz_available(cphf_ctx* c) {
   static bool attr_ok = false, tried = false;
   if (!tried) {
     tried = true;
-    attr_ok = set_smem_attr<Exact6, 128>() && set_smem_attr<Exact6c, 128>() && set_smem_attr<Split2, 128>();
+    attr_ok = set_smem_attr<Exact6, 128>() && set_smem_attr<Exact6c, 128>() && set_smem_attr<Exact6c3, 128>() &&
+              set_smem_attr<Split2, 128>();
     if (!attr_ok) cudaGetLastError();
   }
   return attr_ok;
@@ -1194,7 +1403,11 @@ static void oz_prepare_spin(cphf_ctx* c, OzState& z, int s) {
 template <class PC>
 static void oz_k_terms_t(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, double alpha,
                          double* out) {
-  constexpr bool corr = PC::S == 4;  // correction precision (profiled as its own classes)
+  // correction precisions are profiled as their own classes
+  constexpr int kP = PC::S == 6 ? PROF_TC_OZAKI : PC::S == 4 ? PROF_OZC_KTERM : PROF_OZC3_KTERM;
+  constexpr int tP = PC::S == 6 ? PROF_OZ_TGEN : PC::S == 4 ? PROF_OZC_TGEN : PROF_OZC3_TGEN;
+  constexpr int wP = PC::S == 6 ? PROF_OZ_WGEN : PC::S == 4 ? PROF_OZC_WGEN : PROF_OZC3_WGEN;
+  constexpr int qP = PC::S == 6 ? PROF_OZ_TERM2 : PC::S == 4 ? PROF_OZC_TERM2 : PROF_OZC3_TERM2;
   const int64_t nao = c->nao, naux = c->naux, no = c->spin[s].nocc;
   const int64_t N = no * nb;
   if (N <= 0 || nao <= 0) return;
@@ -1255,7 +1468,7 @@ static void oz_k_terms_t(cphf_ctx* c, OzState& z, int s, const double* bra, int6
       a.e_col = os.eO.as<int>();
       a.m_div = nao; a.s_m1 = 1; a.s_m2 = ldk * no; a.s_n = ldk; a.s_p = N * ldk;
       a.colmax = z.mxc.as<unsigned long long>();  // T's column maxima, reduced in the epilogue
-      ProfScope ps(c, (corr ? PROF_OZC_TGEN : PROF_OZ_TGEN), 2.0 * nao * nb * no * no * npc, 0.0);
+      ProfScope ps(c, tP, 2.0 * nao * nb * no * no * npc, 0.0);
       a.np = (int)npc;
       CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
       launch_batched<PC, EPI_STOREMAX>(c, mBt, mO, a);
@@ -1264,8 +1477,8 @@ static void oz_k_terms_t(cphf_ctx* c, OzState& z, int s, const double* bra, int6
       ProfScope ps_slice(c, PROF_SLICE_EXACT, 0.0, (double)rows * (8.0 * nao + 2.0 * PC::S * ldk));
       exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true, 0,
                                                            z.e_col.as<int>(), z.colscale.as<double>());
-      slice_staging_kernel<PC, float2><<<grid_for(rows * nao), 256, 0, c->stream>>>(z.T.as<float2>(), rows, N, ldk, nao,
-                                                                     z.e_col.as<int>(), z.B.as<__nv_bfloat16>());
+      slice_pairs_kernel<PC::S><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(
+          z.T.as<float2>(), rows, N, ldk, (int)nao, z.e_col.as<int>(), z.B.as<__nv_bfloat16>());
       count_launch(2);
     }
     {
@@ -1282,7 +1495,7 @@ static void oz_k_terms_t(cphf_ctx* c, OzState& z, int s, const double* bra, int6
       a.rowscale = z.rowscale.as<double>();
       a.colscale = z.colscale.as<double>();
       a.ld_out = nao;
-      ProfScope ps(c, (corr ? PROF_OZC_KTERM : PROF_TC_OZAKI), 2.0 * nao * N * nao * npc, 2.0 * S * nao * npc * (nao + N));
+      ProfScope ps(c, kP, 2.0 * nao * N * nao * npc, 2.0 * S * nao * npc * (nao + N));
       launch_split<PC, 128>(c, z, mCd, mT, a);
     }
     {
@@ -1296,20 +1509,20 @@ static void oz_k_terms_t(cphf_ctx* c, OzState& z, int s, const double* bra, int6
       a.e_row = z.ebraw.as<int>();
       a.e_col = os.eZ.as<int>();
       a.m_div = no; a.s_m1 = 1; a.s_m2 = ldj * no; a.s_n = ldj; a.s_p = N * ldj;
-      ProfScope ps(c, (corr ? PROF_OZC_WGEN : PROF_OZ_WGEN), 2.0 * N * no * nao * npc, 0.0);
+      // W's staging column (i, a) = i + nocc (row / nocc): its maxima reduced in the epilogue
+      a.colmax = z.mxc.as<unsigned long long>();
+      ProfScope ps(c, wP, 2.0 * N * no * nao * npc, 0.0);
       a.np = (int)npc;
-      launch_batched<PC>(c, mBw, mZ, a);
+      CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
+      launch_batched<PC, EPI_STOREMAX>(c, mBw, mZ, a);
     }
     {
-      ProfScope ps_slice(c, PROF_SLICE_EXACT, 0.0, (double)rows * (16.0 * no + 12.0 * ldj));
-      CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
-      colmax_rows_kernel<float2><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.W.as<float2>(), rows, N, ldj, no,
-                                                                               z.mxc.as<unsigned long long>());
+      ProfScope ps_slice(c, PROF_SLICE_EXACT, 0.0, (double)rows * (8.0 * no + 2.0 * PC::S * ldj));
       exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true, 0,
                                                            z.e_col.as<int>(), z.colscale.as<double>());
-      slice_staging_kernel<PC, float2><<<grid_for(rows * no), 256, 0, c->stream>>>(z.W.as<float2>(), rows, N, ldj, no,
-                                                                     z.e_col.as<int>(), z.Ws.as<__nv_bfloat16>());
-      count_launch(3);
+      slice_pairs_kernel<PC::S><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(
+          z.W.as<float2>(), rows, N, ldj, (int)no, z.e_col.as<int>(), z.Ws.as<__nv_bfloat16>());
+      count_launch(2);
     }
     {
       // term 2: out[mu, n] += alpha sum_{P, j} Z_P[mu, j] W_P[j, n]
@@ -1325,7 +1538,7 @@ static void oz_k_terms_t(cphf_ctx* c, OzState& z, int s, const double* bra, int6
       a.rowscale = os.sZt.as<double>();
       a.colscale = z.colscale.as<double>();
       a.ld_out = nao;
-      ProfScope ps(c, (corr ? PROF_OZC_TERM2 : PROF_OZ_TERM2), 2.0 * nao * N * no * npc, 2.0 * S * no * npc * (nao + N));
+      ProfScope ps(c, qP, 2.0 * nao * N * no * npc, 2.0 * S * no * npc * (nao + N));
       launch_split<PC, 128>(c, z, mZt, mW, a);
     }
   }
@@ -1336,8 +1549,9 @@ static void oz_k_terms_t(cphf_ctx* c, OzState& z, int s, const double* bra, int6
 }
 
 void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, double alpha, double* out,
-                bool correction) {
-  if (correction) oz_k_terms_t<Exact6c>(c, z, s, bra, nb, alpha, out);
+                int correction_slices) {
+  if (correction_slices == 3) oz_k_terms_t<Exact6c3>(c, z, s, bra, nb, alpha, out);
+  else if (correction_slices == 4) oz_k_terms_t<Exact6c>(c, z, s, bra, nb, alpha, out);
   else oz_k_terms_t<Exact6>(c, z, s, bra, nb, alpha, out);
 }
 
@@ -1353,8 +1567,12 @@ static void lp_prepare_spin(cphf_ctx* c, OzState& z, int s) {
   z.mx.ensure((size_t)std::max<int64_t>(nao, 1) * 8, c->counter());
   o.O.ensure((size_t)S2 * naux * no * ldj * 2, c->counter());
   o.eO.ensure((size_t)naux * no * 4, c->counter());
-  slice_rows_kernel<Split2, float><<<grid_warps(naux * no, c->num_sms), 256, 0, c->stream>>>(
-      sp.O32.as<float>(), naux * no, no, 0, no, 0, 1, o.O.as<__half>(), ldj, naux * no * ldj, o.eO.as<int>());
+  // one exponent per aux function (all its rows): the T-generation epilogue then scales a row
+  // of an aux function's T by one factor.  The planes resolve O_P to 2^-38 max |O_P|, which
+  // moves T_P[nu, (i,a)] by at most 2^-38 sum_j |bra| max |O_P| <= 2^-38 of the bound that
+  // scales T's own FP16 planes (their finest step), so T loses nothing it keeps.
+  slice_groups_kernel<Split2, float><<<(unsigned)std::min<int64_t>(naux, 65535), 256, 0, c->stream>>>(
+      sp.O32.as<float>(), naux, no, no, o.O.as<__half>(), ldj, naux * no * ldj, o.eO.as<int>());
   o.Z.ensure((size_t)S2 * naux * no * ldk * 2, c->counter());
   o.eZ.ensure((size_t)naux * no * 4, c->counter());
   slice_rows_kernel<Split2, float><<<grid_warps(naux * no, c->num_sms), 256, 0, c->stream>>>(
@@ -1374,7 +1592,10 @@ static void lp_prepare_spin(cphf_ctx* c, OzState& z, int s) {
   o.Omax.ensure((size_t)naux * 4, c->counter());
   omax_kernel<<<(unsigned)std::min<int64_t>(naux, 65535), 256, 0, c->stream>>>(sp.O32.as<float>(), no * no, naux,
                                                                               o.Omax.as<unsigned>());
-  count_launch(6);
+  o.Zmax.ensure((size_t)naux * 4, c->counter());
+  omax_kernel<<<(unsigned)std::min<int64_t>(naux, 65535), 256, 0, c->stream>>>(sp.Z32.as<float>(), nao * no, naux,
+                                                                              o.Zmax.as<unsigned>());
+  count_launch(7);
   CPHF_CUDA(cudaGetLastError());
   o.ready = true;
 }
@@ -1398,7 +1619,11 @@ void lp_begin(cphf_ctx* c, OzState& z, int s, const float* bra, int64_t nb) {
     z.braS.ensure(sizeof(unsigned), c->counter());
     CPHF_CUDA(cudaMemsetAsync(z.braS.p, 0, sizeof(unsigned), c->stream));
     bra_rowsum_max_kernel<<<grid_for(nao * nb), 256, 0, c->stream>>>(bra, nao, no, nb, z.braS.as<unsigned>());
-    count_launch(3);
+    // max over (j, a) of sum_nu |bra|, for the W bound
+    z.braWS.ensure(sizeof(unsigned), c->counter());
+    CPHF_CUDA(cudaMemsetAsync(z.braWS.p, 0, sizeof(unsigned), c->stream));
+    rowsum_abs_max_kernel<<<grid_warps(N, c->num_sms), 256, 0, c->stream>>>(bra, nao, N, z.braWS.as<unsigned>());
+    count_launch(4);
   }
   CPHF_CUDA(cudaGetLastError());
 }
@@ -1432,7 +1657,11 @@ void lp_tgen_planes(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int
   if (a.nkb <= ResT::MAX_KB && no <= ResT::BN && res_attr_ok()) {
     // bra tile resident, all i of a column in one 128-wide tile
     const CUtensorMap mO128 = make_map(z.spin[s].O.p, no, no, S2 * naux, ldj, ResT::BN, false);
-    launch_tgen_resident(c, mBt, mO128, a);
+    // store maps of the epilogue warps' parts: columns [0, 64) and [64, nocc)
+    const int64_t n0c = std::min<int64_t>(no, 64), n1c = std::max<int64_t>(no - 64, 1);
+    const CUtensorMap mT[4] = {make_t_store_map(hi, nao, N, npc, ldt, n0c), make_t_store_map(hi, nao, N, npc, ldt, n1c),
+                               make_t_store_map(lo, nao, N, npc, ldt, n0c), make_t_store_map(lo, nao, N, npc, ldt, n1c)};
+    launch_tgen_resident(c, mBt, mO128, mT, a);
   } else {
     launch_batched<Split2, EPI_SPLIT16>(c, mBt, mO, a);
   }
@@ -1444,49 +1673,33 @@ void lp_w_term2(cphf_ctx* c, OzState& z, int s, int64_t P0, int64_t npc, int64_t
   const int64_t ldk = z.ldk, ldj = z.spin[s].ldj;
   constexpr int S2 = Split2::S;
   const OzSpin& os = z.spin[s];
-  z.W.ensure((size_t)npc * N * ldj * 4, c->counter());
   z.Ws.ensure((size_t)S2 * npc * N * ldj * 2, c->counter());
-  z.colscale.ensure((size_t)N * 8, c->counter());
-  z.e_col.ensure((size_t)N * 4, c->counter());
-  z.mxc.ensure((size_t)N * 8, c->counter());
-  const int64_t rows = npc * N;
+  z.wsc.ensure(16, c->counter());
+  unsigned* mx = z.wsc.as<unsigned>();
+  float* wscale = reinterpret_cast<float*>(mx + 2);  // [0] = W's plane scale, [1] = alpha / [0]
+  __half* ws = z.Ws.as<__half>();
   {
-    // W-gen: W[Pl][(i,a)][j], rows m = j + no a, columns i, K = nu
-    const CUtensorMap mBw = make_map(z.braw.p, nao, N, S2, ldk, BM, false);
-    const CUtensorMap mZ = make_map(os.Z.p, nao, no, S2 * naux, ldk, 64, false);
-    OzArgs a = base_args(z, (int)N, (int)no);
-    a.err = err;
-    a.out = z.W.p;
-    a.nkb = (int)div_up(nao, BK);
-    a.a_depth = 1;
-    a.b_depth = (int)naux;
-    a.b_off = (int)P0;
-    a.e_row = z.ebraw.as<int>();
-    a.e_col = os.eZ.as<int>();
-    a.m_div = no; a.s_m1 = 1; a.s_m2 = ldj * no; a.s_n = ldj; a.s_p = N * ldj;
-    ProfScope ps(c, PROF_TC_WGEN, 2.0 * N * no * nao * npc, 0.0);
-    a.np = (int)npc;
-    launch_batched<Split2>(c, mBw, mZ, a);
-  }
-  {
-    ProfScope ps_slice(c, PROF_SLICE, 0.0, (double)rows * (8.0 * no + 4.0 * ldj));
-    CPHF_CUDA(cudaMemsetAsync(z.mxc.p, 0, (size_t)N * 8, c->stream));
-    colmax_rows_kernel<float><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(z.W.as<float>(), rows, N, ldj, no,
-                                                                                    z.mxc.as<unsigned long long>());
-    exp_scale_kernel<<<grid_for(N), 256, 0, c->stream>>>(z.mxc.as<unsigned long long>(), N, alpha, true, Split2::EOFF,
-                                                         z.e_col.as<int>(), z.colscale.as<double>());
-    slice_staging_kernel<Split2, float><<<grid_for(rows * no), 256, 0, c->stream>>>(
-        z.W.as<float>(), rows, N, ldj, no, z.e_col.as<int>(), z.Ws.as<__half>());
-    count_launch(3);
+    // W-gen: FP16 planes of W_P[(j,a), i] * wscale into Ws[Pl][a][i][j] as one GEMM over the
+    // chunk (rows (j, a), columns (i, Pl), K = nu); the scale from the upper bound
+    // |W| <= max_(j,a) sum_nu |bra| * max_P |Z_P|, so no FP32 staging and no max pass
+    ProfScope ps(c, PROF_TC_WGEN, 2.0 * N * no * nao * npc, 2.0 * S2 * (N + no * npc) * nao + 2.0 * S2 * npc * N * no);
+    tbound_kernel<<<1, 256, 0, c->stream>>>(z.braWS.as<unsigned>(), os.Zmax.as<unsigned>() + P0, npc, mx);
+    count_launch();
+    launch_t_scale(mx, 1.f, (float)alpha, wscale, c->stream);
+    const __half* zp = os.Z.as<__half>();
+    const __half* bw = z.braw.as<__half>();
+    tc_wgen_planes(c, bw, bw + N * ldk, N, zp, zp + naux * no * ldk, no * naux, no * P0, no * npc, nao, ldk,
+                   z.ebraw.as<int>(), os.eZ.as<int>(), wscale, no, ldj, ldj * no, N * ldj, ws, ws + npc * N * ldj,
+                   err);
   }
   {
     // term 2: out[mu, n] += alpha sum_{P, j} Z_P[mu, j] W_P[j, n] on the term-1 kernel's 256-wide
-    // tiles (K = j per aux function in 64-wide blocks), rows scaled by Z^T's, columns by W's scales
+    // tiles (K = j per aux function in 64-wide blocks), rows scaled by Z^T's scales, every
+    // element by alpha / wscale
     ProfScope ps(c, PROF_TC_TERM2, 2.0 * nao * N * no * npc, 2.0 * S2 * no * npc * (nao + N));
     const __half* zt = os.Zt.as<__half>();
-    const __half* ws = z.Ws.as<__half>();
     tc_planes_term(c, zt, zt + naux * nao * ldj, naux, P0, ws, ws + npc * N * ldj, npc, nao, N, no, ldj,
-                   os.sZt.as<double>(), z.colscale.as<double>(), out, nao, err);
+                   os.sZt.as<double>(), nullptr, out, nao, err, wscale + 1);
   }
 }
 

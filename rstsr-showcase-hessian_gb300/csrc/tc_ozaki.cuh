@@ -19,10 +19,11 @@ bool oz_supported(const cphf_ctx* c);
 // row-scaled 6-slice BF16 copy of the dense cderi (once per cderi)
 void oz_prepare_cderi(cphf_ctx* c, OzState& z);
 // out (FP64 [nao, nocc_s, nb], initialised) += alpha * K-term of spin s;
-// bra FP64 [nao, nocc_s, nb].  correction: the contractions read slices 0-3 only (10 products,
-// ~2^-24 relative to the operands' maxima), for a bra that is a small correction.
+// bra FP64 [nao, nocc_s, nb].  correction_slices 4 / 3: the contractions read slices 0-3 /
+// 0-2 only (10 / 6 products, ~2^-23 / ~2^-17 relative to the operands' maxima), for a bra that
+// is a small correction; 0: all six (21 products).
 void oz_k_terms(cphf_ctx* c, OzState& z, int s, const double* bra, int64_t nb, double alpha, double* out,
-                bool correction = false);
+                int correction_slices = 0);
 
 // Split-FP16 (hi/lo, three products, FP32 accumulation) contractions of the K term for the
 // inner solves' operator, from the FP32 copies of O and Z:

@@ -239,6 +239,15 @@ def test_lowp_operator_accuracy(dims, tc):
         assert "kterm_tcgen05_f16x3" not in clp.profile_report()
 
 
+def assert_correction_classes(ctx):
+    """Some residual update ran on the exact-slice operator in correction precision (3 or 4
+    slices), all four of its contractions on tcgen05."""
+    rep = ctx.profile_report()
+    assert any(rep.get(f"kterm_tcgen05_bf16x{k}c_exact", {}).get("launches", 0) > 0 for k in (3, 4)), sorted(rep)
+    for part in ("kterm", "tgen", "wgen", "term2"):
+        assert sum(rep.get(f"{part}_tcgen05_bf16x{k}c_exact", {}).get("launches", 0) for k in (3, 4)) > 0, part
+
+
 def assert_tensor_core_classes(ctx, classes):
     """The context ran its split-precision / exact-slice contractions on tcgen05: the tensor
     cores are active and each named kernel class of the CUDA-event profiler has launches."""
@@ -307,8 +316,9 @@ def test_mixed_precision_solve(dims, dfloat):
     # subtracted with the exact-slice operator in correction precision (residual mode 4)
     assert st["residual_mode"] == (4 if dfloat == 2 and st["refine_steps"] > 1 else dfloat)
     if dfloat == 2:
-        assert_tensor_core_classes(cmx, ["kterm_tcgen05_f16x3", "kterm_tcgen05_bf16x6_exact",
-                                         "kterm_tcgen05_bf16x4c_exact"])
+        assert_tensor_core_classes(cmx, ["kterm_tcgen05_f16x3", "kterm_tcgen05_bf16x6_exact"])
+        if st["refine_steps"] > 1:
+            assert_correction_classes(cmx)
     res64, xmax = _max_col_residual(c64, s, xmx)
     assert res64 < 1e-8
     # the solve's own final residual agrees with the native FP64 residual of its answer
@@ -324,6 +334,27 @@ def test_mixed_precision_solve(dims, dfloat):
         m1, me = ctx.finalize_cphf(f1, s1, x[0] if s.nspin == 1 else x)
         h.append(ctx.get_cphf_hess(f1, s1, m1, me))
     assert np.abs(h[0] - h[1]).max() < 1e-7
+
+
+@pytest.mark.parametrize("dims", [MEDIUM, TC_RAGGED, MEDIUM_U])
+def test_correction_precision_residual(dims):
+    """Loose inner solves force several defect-correction steps: every later residual is the
+    previous one minus (I + A) d on the exact-slice operator in correction precision (residual
+    mode 4), and the solve's own final residual still agrees with the native FP64 residual."""
+    s = synth.make_system(dims, seed=21)
+    rhs = s.rhs[0] if s.nspin == 1 else s.rhs
+    c64 = make_ctx(s)
+    cmx = make_ctx(s, precision="mixed", residual_dfloat=2, inner_tol=1e-3)
+    cmx.profile(True)
+    x = cmx.solve_dimless_cphf(rhs)
+    st = cmx.last_stats
+    assert st["refine_steps"] >= 2 and st["residual_mode"] == 4
+    assert st["residual_max"] < 1e-8
+    assert_tensor_core_classes(cmx, ["kterm_tcgen05_bf16x6_exact"])
+    assert_correction_classes(cmx)
+    res64, xmax = _max_col_residual(c64, s, x)
+    assert res64 < 1e-8
+    assert abs(st["residual_max"] - res64) < 1e-9 * max(1.0, xmax), (st["residual_max"], res64)
 
 
 @pytest.mark.parametrize("dims", [MEDIUM, GRID_U])
