@@ -623,6 +623,8 @@ def run_gpu(args, world, rank, local):
         "tgen_tcgen05_bf16x3c_exact": "exact BF16 slices in correction precision, 6 slice products",
         "wgen_tcgen05_bf16x3c_exact": "exact BF16 slices in correction precision, 6 slice products",
         "term2_tcgen05_bf16x3c_exact": "exact BF16 slices in correction precision, 6 slice products",
+        "xc_tcgen05_bf16c_exact": "per grid batch over its AO window, exact BF16 slices in correction precision "
+                                  "(3 or 4 slices, 6 or 10 products)",
     }
     if dom_name in ("slice_scale_split", "slice_exact"):
         roof = dict(bound="hbm", achieved=dom["bytes"] / dom["ms"] / 1e6, peak=hbm, unit="GB/s",
@@ -640,7 +642,7 @@ def run_gpu(args, world, rank, local):
                                  f"counts algorithmic FLOPs") + (f"; {note}" if note else ""))
     # DRAM bytes per launch: the ratio of ncu-measured DRAM bytes to the algorithmic bytes of
     # the same kernel on a small case (profiles/), times this run's algorithmic bytes per launch
-    traffic_ratio = {"kterm_tcgen05_f16x3": 1.262 / 1.18,        # tc_term1_kernel, rhf_nao300
+    traffic_ratio = {"kterm_tcgen05_f16x3": 9.99 / 9.25,         # tc_term1_kernel, rhf_nao384_occ120
                      "kterm_tcgen05_bf16x6_exact": 5.954 / 5.22}  # tc_slice_kernel<Exact6>, rhf_nao300
     traffic = None
     if dom_name in traffic_ratio and dom.get("bytes", 0) > 0:

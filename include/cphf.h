@@ -58,7 +58,10 @@ typedef struct cphf_config {
   int32_t precision;         /* cphf_precision, default CPHF_PRECISION_FP64 */
   int32_t device;            /* CUDA device ordinal, default 0 */
   double residual_tol;       /* mixed: stop when max column ||b-(I+A)x||_2 < residual_tol (default 1e-8) */
-  double inner_tol;          /* mixed: Krylov tol of each inner solve, relative to the residual (default 1e-6) */
+  double inner_tol;          /* mixed: Krylov tol of the first inner solve, relative to the residual (default
+                                1e-6); later inner solves use max(inner_tol, min(1e-2, 0.1 q residual_tol / |r|)),
+                                the reduction that the remaining residual |r| still needs (q = min |m| / max |m|
+                                under a learned preconditioner m, else 1) */
   int64_t max_refine;        /* mixed: maximum defect-correction steps (default 6) */
   int32_t use_learned_guess; /* learned per-pair MLP (weights set by cphf_mlp_set_weights), default 0 = off.
                                 MIXED: 1 = left preconditioner of the inner solves, 2 = preconditioner and

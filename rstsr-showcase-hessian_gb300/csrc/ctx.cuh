@@ -190,7 +190,8 @@ enum ProfClass {
   PROF_OZC3_TGEN = 23,
   PROF_OZC3_WGEN = 24,
   PROF_OZC3_TERM2 = 25,
-  PROF_NCLASS = 26
+  PROF_XC_TC64C = 26,
+  PROF_NCLASS = 27
 };
 extern const char* const kProfNames[PROF_NCLASS];
 

@@ -169,28 +169,32 @@ __global__ void mgs_init_kernel(const double* __restrict__ V, int64_t n, int64_t
   }
 }
 
-// Reduce partials of step i: ip[i], keep[i], coef[j] for j > i.
+// sum of the nblk partials of column j: one warp, lanes over blocks, then a shuffle tree
+__device__ __forceinline__ double mgs_sum(const double* __restrict__ partials, int64_t nblk, int64_t j, int lane) {
+  double s = 0.0;
+  for (int64_t k = lane; k < nblk; k += 32) s += partials[k + nblk * j];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  return s;
+}
+
+// Reduce partials of step i: ip[i], keep[i], coef[j] for j > i.  One warp per column (every
+// warp first forms the squared norm of column i itself, so that no block waits on another).
 __global__ void mgs_reduce_kernel(const double* __restrict__ partials, int64_t nblk, int64_t m,
                                   int64_t i, double lindep, double* __restrict__ ip,
                                   int* __restrict__ keep, double* __restrict__ coef) {
-  __shared__ double nsq_sh;
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int64_t k = 0; k < nblk; ++k) s += partials[k + nblk * i];
-    nsq_sh = s;
-    ip[i] = s;
-    keep[i] = (s > lindep) ? 1 : 0;
-  }
-  __syncthreads();
-  const double nsq = nsq_sh;
+  const int lane = threadIdx.x & 31;
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const double nsq = mgs_sum(partials, nblk, i, lane);
   const bool kept = nsq > lindep;
-  for (int64_t j = i + 1 + threadIdx.x; j < m; j += blockDim.x) {
+  if (w == 0 && lane == 0) {
+    ip[i] = nsq;
+    keep[i] = kept ? 1 : 0;
+  }
+  for (int64_t j = i + 1 + w; j < m; j += nw) {
     double s = 0.0;
-    if (kept) {
-      for (int64_t k = 0; k < nblk; ++k) s += partials[k + nblk * j];
-      s /= nsq;
-    }
-    coef[j] = s;
+    if (kept) s = mgs_sum(partials, nblk, j, lane) / nsq;
+    if (lane == 0) coef[j] = s;
   }
 }
 
@@ -434,13 +438,46 @@ void launch_mgs(double* V, int64_t n, int64_t m, double lindep, double* ip, int*
   mgs_init_kernel<<<(unsigned)g.nblk, kThreads, 0, s>>>(V, n, m, 0, g.rows, partials);
   count_launch();
   for (int64_t i = 0; i < m; ++i) {
-    mgs_reduce_kernel<<<1, kThreads, 0, s>>>(partials, g.nblk, m, i, lindep, ip, keep, coef);
+    // one warp per remaining column (8 per block)
+    const unsigned rblocks = (unsigned)std::max<int64_t>(1, div_up(m - i, 8));
+    mgs_reduce_kernel<<<rblocks, 256, 0, s>>>(partials, g.nblk, m, i, lindep, ip, keep, coef);
     count_launch();
     if (i + 1 < m) {
       mgs_update_kernel<<<(unsigned)g.nblk, kThreads, 0, s>>>(V, n, m, i, g.rows, coef, keep, partials);
       count_launch();
     }
   }
+}
+
+namespace {
+// |x| of non-negative doubles orders like their bit patterns: min / max by integer atomics
+__global__ void abs_minmax_kernel(const double* __restrict__ x, int64_t n, unsigned long long* out) {
+  unsigned long long lo = ~0ull, hi = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long k = (unsigned long long)__double_as_longlong(x[i]) & 0x7FFFFFFFFFFFFFFFull;
+    lo = min(lo, k);
+    hi = max(hi, k);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(out, lo);
+    atomicMax(out + 1, hi);
+  }
+}
+__global__ void minmax_init_kernel(unsigned long long* out) {
+  out[0] = ~0ull;
+  out[1] = 0;
+}
+}  // namespace
+
+void launch_abs_minmax(const double* x, int64_t n, double* out, cudaStream_t s) {
+  unsigned long long* o = reinterpret_cast<unsigned long long*>(out);
+  minmax_init_kernel<<<1, 1, 0, s>>>(o);
+  abs_minmax_kernel<<<grid_for(n), kThreads, 0, s>>>(x, n, o);
+  count_launch(2);
 }
 
 void launch_gather_cols(const double* src, int64_t n, const int* idx, int64_t cnt, double* dst,

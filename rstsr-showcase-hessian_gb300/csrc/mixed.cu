@@ -367,7 +367,7 @@ AccurateScope::AccurateScope(cphf_ctx* ctx, int mode, int correction_slices) : c
   c->f64_emulate = mode != 0;
   c->oz_kterm = mode == 2 && c->has_rijk && tc && oz_supported(c);
   c->oz_xc = mode == 2 && c->has_xc && c->xc_den == 0 && tc;  // the tensor-core XC covers LDA
-  c->oz_correction = c->oz_kterm ? correction_slices : 0;
+  c->oz_correction = (c->oz_kterm || c->oz_xc) ? correction_slices : 0;
   c->f32_correction = c->oz_correction != 0;  // the correction's J, C x and C^T r GEMMs to ~1e-7 of it
   // mode 2 without any tensor-core contraction available is the double-float operator
   used = mode == 2 && !(c->oz_kterm || c->oz_xc) ? 1 : mode;
@@ -409,6 +409,17 @@ bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, d
   for (double v : h) res = std::max(res, std::sqrt(v));
   const KrylovParams p{c->cfg.inner_tol, c->cfg.cphf_lindep, c->cfg.cphf_max_cycle, c->cfg.cphf_max_space,
                        c->cfg.verbose != 0};
+  // a left preconditioner m turns the inner stopping test into one on m r: the true residual
+  // is then bounded only up to max |m| / min |m|, which the later steps' tolerance folds in
+  double m_ratio = 1.0;
+  bool loosen = true, loosened = false;
+  if (m) {
+    double mm[2];
+    launch_abs_minmax(m, n, c->k_norm.as<double>(), s);
+    CPHF_CUDA(cudaMemcpyAsync(mm, c->k_norm.p, 16, cudaMemcpyDeviceToHost, s));
+    CPHF_CUDA(cudaStreamSynchronize(s));
+    m_ratio = (mm[1] > 0.0 && std::isfinite(mm[1])) ? mm[0] / mm[1] : 0.0;
+  }
   DeviceOp op = [&](const double* xin, int64_t nb, double* yout) {
     lowp_apply(c, xin, nb, yout);
     if (m) launch_apply_precond(m, xin, yout, n, nb, c->stream);
@@ -444,7 +455,18 @@ bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, d
     // the inner solve's Gram / projection GEMMs in double-float (its operator is ~1e-6 accurate)
     c->f64_emulate = c->cfg.residual_dfloat != 0;
     try {
-      krylov_device(c, op, rr, g0, n, nset, p, dlt, st);
+      // Later corrections need only bring the residual below the target: relative tolerance
+      // 0.1 residual_tol / |r| (within [inner_tol, 1e-2], times min |m| / max |m| under a
+      // preconditioner) instead of inner_tol.  At nao 600-800 this saves the second inner
+      // cycle of step 1 (one operator application of six); the final residual then sits
+      // ~1e-10 instead of ~1e-11, still 100x below the target.
+      // A loosened step that does not reach the target turns the loosening off for the rest
+      // of the solve (a poor preconditioner can make the inner test on m r too optimistic).
+      KrylovParams pk = p;
+      loosened = step > 0 && res > 0.0 && loosen;
+      if (loosened)
+        pk.tol = std::max(c->cfg.inner_tol, std::min(1e-2, 0.1 * m_ratio * c->cfg.residual_tol / res));
+      krylov_device(c, op, rr, g0, n, nset, pk, dlt, st);
     } catch (...) {
       c->f64_emulate = false;
       throw;
@@ -503,6 +525,7 @@ bool solve_mixed(cphf_ctx* c, const double* b, const double* x0, int64_t nset, d
       done = res < update_margin * c->cfg.residual_tol;
       how = "updated";
     }
+    if (loosened && !done) loosen = false;
     if (c->cfg.verbose)
       std::printf("defect correction step %lld: max ||b - (I+A)x|| = %.3e (%s, mode %lld)\n", (long long)step + 1,
                   res, how, (long long)st->residual_mode);

@@ -34,7 +34,8 @@ const char* const kProfNames[PROF_NCLASS] = {"gemm_fp64_simt", "gemm_fp32_simt",
                                              "tgen_tcgen05_bf16x4c_exact", "wgen_tcgen05_bf16x4c_exact",
                                              "term2_tcgen05_bf16x4c_exact", "slice_exact",
                                              "kterm_tcgen05_bf16x3c_exact", "tgen_tcgen05_bf16x3c_exact",
-                                             "wgen_tcgen05_bf16x3c_exact", "term2_tcgen05_bf16x3c_exact"};
+                                             "wgen_tcgen05_bf16x3c_exact", "term2_tcgen05_bf16x3c_exact",
+                                             "xc_tcgen05_bf16c_exact"};
 
 static double gemm_flops(const GemmDesc& d) { return 2.0 * d.M * d.N * d.K * d.batch1 * d.batch2; }
 

@@ -92,10 +92,11 @@ __device__ __forceinline__ void digits6(long long F, bool bad, __nv_bfloat16* ds
     dst[t * plane] = __float2bfloat16_rn(v);
   }
 }
+template <int NS = 6>
 __device__ __forceinline__ void slice6(double x, int e, __nv_bfloat16* dst, int64_t plane) {
   bool bad = false;
   const long long F = fix_round(x, 36 - e, bad);
-  digits6(F, bad, dst, plane);
+  digits6<NS>(F, bad, dst, plane);
 }
 // Digits of an FP32 pair v = x.x + x.y (|v| < 2^e) in FP32 arithmetic: the balanced base-64
 // digits of F ~ v 2^(36 - e) (|F - v 2^(36 - e)| <= 1/2 + 2^-6), the same representation as
@@ -150,6 +151,7 @@ struct Put<Exact6> {
 template <int NS>
 struct Put<ExactC<NS>> {  // only the planes a correction-precision product reads
   __device__ static void put(float2 x, int e, __nv_bfloat16* dst, int64_t plane) { slice6<NS>(x, e, dst, plane); }
+  __device__ static void put(double x, int e, __nv_bfloat16* dst, int64_t plane) { slice6<NS>(x, e, dst, plane); }
 };
 template <>
 struct Put<Split2> {

@@ -667,11 +667,20 @@ struct ResT {
 };
 
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, uint32_t src, int c0, int c1, int c2) {
-  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
-                   reinterpret_cast<uint64_t>(map)),
-               "r"(src), "r"(c0), "r"(c1), "r"(c2)
-               : "memory");
+// L2 policy that evicts the lines written first (T is streamed: read once, by term 1, after
+// the chunk is complete), so that the O tiles the next aux functions read stay in L2
+__device__ __forceinline__ uint64_t l2_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, uint32_t src, int c0, int c1, int c2,
+                                             uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.global.shared::cta.bulk_group.L2::cache_hint [%0, {%2, %3, %4}], [%1], %5;" ::"l"(
+          reinterpret_cast<uint64_t>(map)),
+      "r"(src), "r"(c0), "r"(c1), "r"(c2), "l"(policy)
+      : "memory");
 }
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
@@ -797,6 +806,7 @@ __global__ void __launch_bounds__(320, 1)
       __half* const sl = sh + 64 * 32;
       const CUtensorMap* const mh = h == 0 ? &mTh0 : &mTh1;
       const CUtensorMap* const ml = h == 0 ? &mTl0 : &mTl1;
+      const uint64_t policy = l2_evict_first();
       for (int p = 0; p < nP; ++p) {
         const int b = p & 1;
         const int e_p = e_next;
@@ -841,8 +851,8 @@ __global__ void __launch_bounds__(320, 1)
         __syncwarp();
         if (lane == 0 && nu0 + 32 * q < nao) {  // (a box wholly past nu = nao has nothing to store)
           const int Pl = p_begin + p;
-          tma_store_3d(mh, smem_u32(wst), nu0 + 32 * q, a_pert * no + 64 * h, Pl);
-          tma_store_3d(ml, smem_u32(wst + ResT::WARP_OUT / 2), nu0 + 32 * q, a_pert * no + 64 * h, Pl);
+          tma_store_3d(mh, smem_u32(wst), nu0 + 32 * q, a_pert * no + 64 * h, Pl, policy);
+          tma_store_3d(ml, smem_u32(wst + ResT::WARP_OUT / 2), nu0 + 32 * q, a_pert * no + 64 * h, Pl, policy);
           bulk_commit();
         }
       }
@@ -1769,12 +1779,35 @@ void oz_gemm(cphf_ctx* c, OzState& z, const PlaneMat& A, int64_t a_row0, const P
   plane_gemm<Exact6>(c, z, A, a_row0, B, b_k0, M, N, K, rowscale, colscale, out, ld_out, err, kb_per_cta, store);
 }
 
+void oz_gemm_corr(cphf_ctx* c, OzState& z, int slices, const PlaneMat& A, int64_t a_row0, const PlaneMat& B,
+                  int64_t b_k0, int64_t M, int64_t N, int64_t K, const double* rowscale, const double* colscale,
+                  double* out, int64_t ld_out, int* err, int kb_per_cta, bool store) {
+  if (slices == 3)
+    plane_gemm<Exact6c3>(c, z, A, a_row0, B, b_k0, M, N, K, rowscale, colscale, out, ld_out, err, kb_per_cta, store);
+  else
+    plane_gemm<Exact6c>(c, z, A, a_row0, B, b_k0, M, N, K, rowscale, colscale, out, ld_out, err, kb_per_cta, store);
+}
+
 // Split-FP16 planes [t][r][ld] of FP32 rows r (K elements each, row stride rs), exponents to e_out.
 void lp_slice_rows(cphf_ctx* c, const float* src, int64_t rows, int64_t K, int64_t rs, __half* dst, int64_t ld,
                    int* e_out) {
   ProfScope ps_slice(c, PROF_SLICE, 0.0, 4.0 * rows * K + 4.0 * rows * ld);
   slice_rows_kernel<Split2, float><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(
       src, rows, K, 0, rs, 0, 1, dst, ld, rows * ld, e_out);
+  count_launch();
+  CPHF_CUDA(cudaGetLastError());
+}
+
+// The leading `slices` (3 or 4) of the same planes, for correction-precision contractions.
+void oz_slice_rows_corr(cphf_ctx* c, int slices, const double* src, int64_t rows, int64_t K, int64_t rs,
+                        __nv_bfloat16* dst, int64_t ld, int* e_out) {
+  ProfScope ps_slice(c, PROF_SLICE, 0.0, 8.0 * rows * K + 2.0 * slices * rows * ld);
+  if (slices == 3)
+    slice_rows_kernel<Exact6c3, double><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(
+        src, rows, K, 0, rs, 0, 1, dst, ld, rows * ld, e_out);
+  else
+    slice_rows_kernel<Exact6c, double><<<grid_warps(rows, c->num_sms), 256, 0, c->stream>>>(
+        src, rows, K, 0, rs, 0, 1, dst, ld, rows * ld, e_out);
   count_launch();
   CPHF_CUDA(cudaGetLastError());
 }

@@ -78,5 +78,12 @@ void oz_gemm(cphf_ctx* c, OzState& z, const PlaneMat& A, int64_t a_row0, const P
 // exact BF16 slice planes [t][r][ld] of FP64 rows r (K elements each, row stride rs); exponents to e_out
 void oz_slice_rows(cphf_ctx* c, const double* src, int64_t rows, int64_t K, int64_t rs, __nv_bfloat16* dst,
                    int64_t ld, int* e_out);
+// the same contraction and slicer in correction precision: the leading `slices` (3 or 4) planes,
+// the products with t + u < slices
+void oz_gemm_corr(cphf_ctx* c, OzState& z, int slices, const PlaneMat& A, int64_t a_row0, const PlaneMat& B,
+                  int64_t b_k0, int64_t M, int64_t N, int64_t K, const double* rowscale, const double* colscale,
+                  double* out, int64_t ld_out, int* err, int kb_per_cta = 0, bool store = false);
+void oz_slice_rows_corr(cphf_ctx* c, int slices, const double* src, int64_t rows, int64_t K, int64_t rs,
+                        __nv_bfloat16* dst, int64_t ld, int* e_out);
 
 }  // namespace cphf

@@ -226,6 +226,21 @@ struct XcOps<Exact6> {
   }
 };
 
+template <int NS>
+struct XcOps<ExactC<NS>> {  // correction precision: the leading NS planes of the exact slices
+  using T = double;
+  static constexpr int PROF = PROF_XC_TC64C;
+  static void gemm(cphf_ctx* c, OzState& z, const PlaneMat& A, int64_t a_row0, const PlaneMat& B, int64_t b_k0,
+                   int64_t M, int64_t N, int64_t K, const double* rs, const double* cs, double* out, int64_t ld_out,
+                   int* err, int kb_per_cta, bool store) {
+    oz_gemm_corr(c, z, NS, A, a_row0, B, b_k0, M, N, K, rs, cs, out, ld_out, err, kb_per_cta, store);
+  }
+  static void slice(cphf_ctx* c, const double* src, int64_t rows, int64_t K, int64_t rs, __nv_bfloat16* dst,
+                    int64_t ld, int* e) {
+    oz_slice_rows_corr(c, NS, src, rows, K, rs, dst, ld, e);
+  }
+};
+
 // Batch records and the phi planes of the grid (once per grid).
 template <class PR, class T>
 void xc_tc_prepare(cphf_ctx* c, XcTcState& X, const T* phi) {
@@ -296,7 +311,9 @@ void xc_tc(cphf_ctx* c, XcTcState& X, OzState& z, const typename XcOps<PR>::T* p
       if (c->spin[s].nocc > 0)
         CPHF_CUDA(cudaMemsetAsync(out[s], 0, (size_t)nao * c->spin[s].nocc * nb * sizeof(T), st));
   if (nb <= 0 || c->xc_batches.empty()) return;
-  if (!X.ready) xc_tc_prepare<PR, T>(c, X, phi);
+  // correction precision reads the leading planes of the exact slices' phi planes
+  using PREP = std::conditional_t<(PR::NACC == 4 && PR::S < 6), Exact6, PR>;
+  if (!X.ready) xc_tc_prepare<PREP, T>(c, X, phi);
   const XcPlan& pl = xc_plan(c, sizeof(T), nb);
   int64_t ket_spin[2] = {0, 0};
   for (int s = 0; s < ns; ++s) ket_spin[s] = pl.max_pts * c->spin[s].nocc * nb;
@@ -426,8 +443,16 @@ void xc_response_tc64(cphf_ctx* c, const double* const* bra, int64_t nb, double*
   z.err.ensure(sizeof(int), c->counter());
   CPHF_CUDA(cudaMemsetAsync(z.err.p, 0, sizeof(int), c->stream));
   const double* aobra[2] = {c->spin[0].aobra.as<double>(), c->nspin > 1 ? c->spin[1].aobra.as<double>() : nullptr};
-  xc_tc<Exact6>(c, L.xctc64, z, c->phi.as<double>(), aobra, c->s_ket, c->s_rho, bra, nb, out, accumulate,
-                z.err.as<int>());
+  // a correction-precision application (3 or 4 slices) shares the exact slices' grid planes
+  if (c->oz_correction == 3)
+    xc_tc<Exact6c3>(c, L.xctc64, z, c->phi.as<double>(), aobra, c->s_ket, c->s_rho, bra, nb, out, accumulate,
+                    z.err.as<int>());
+  else if (c->oz_correction == 4)
+    xc_tc<Exact6c>(c, L.xctc64, z, c->phi.as<double>(), aobra, c->s_ket, c->s_rho, bra, nb, out, accumulate,
+                   z.err.as<int>());
+  else
+    xc_tc<Exact6>(c, L.xctc64, z, c->phi.as<double>(), aobra, c->s_ket, c->s_rho, bra, nb, out, accumulate,
+                  z.err.as<int>());
   int flag = 0;
   CPHF_CUDA(cudaMemcpyAsync(&flag, z.err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CPHF_CUDA(cudaStreamSynchronize(c->stream));

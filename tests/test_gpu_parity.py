@@ -336,7 +336,7 @@ def test_mixed_precision_solve(dims, dfloat):
     assert np.abs(h[0] - h[1]).max() < 1e-7
 
 
-@pytest.mark.parametrize("dims", [MEDIUM, TC_RAGGED, MEDIUM_U])
+@pytest.mark.parametrize("dims", [MEDIUM, TC_RAGGED, MEDIUM_U, GRID_R, GRID_U])
 def test_correction_precision_residual(dims):
     """Loose inner solves force several defect-correction steps: every later residual is the
     previous one minus (I + A) d on the exact-slice operator in correction precision (residual
@@ -352,6 +352,8 @@ def test_correction_precision_residual(dims):
     assert st["residual_max"] < 1e-8
     assert_tensor_core_classes(cmx, ["kterm_tcgen05_bf16x6_exact"])
     assert_correction_classes(cmx)
+    if s.grid is not None:  # the XC grid contractions of the corrections in correction precision too
+        assert_tensor_core_classes(cmx, ["xc_tcgen05_bf16x6_exact", "xc_tcgen05_bf16c_exact"])
     res64, xmax = _max_col_residual(c64, s, x)
     assert res64 < 1e-8
     assert abs(st["residual_max"] - res64) < 1e-9 * max(1.0, xmax), (st["residual_max"], res64)
