@@ -59,14 +59,14 @@ typedef struct cphf_config {
   int32_t device;            /* CUDA device ordinal, default 0 */
   double residual_tol;       /* mixed: stop when max column ||b-(I+A)x||_2 < residual_tol (default 1e-8) */
   double inner_tol;          /* mixed: Krylov tol of the first inner solve, relative to the residual (default
-                                1e-6); later inner solves use max(inner_tol, min(1e-2, 0.1 q residual_tol / |r|)),
-                                the reduction that the remaining residual |r| still needs (q = min |m| / max |m|
-                                under a learned preconditioner m, else 1) */
+                                1e-6); later inner solves use max(inner_tol, min(1e-2, 0.1 residual_tol / |r|)),
+                                the reduction that the remaining residual |r| still needs (until one of them
+                                misses the target) */
   int64_t max_refine;        /* mixed: maximum defect-correction steps (default 6) */
   int32_t use_learned_guess; /* learned per-pair MLP (weights set by cphf_mlp_set_weights), default 0 = off.
-                                MIXED: 1 = left preconditioner of the inner solves, 2 = preconditioner and
-                                initial guess of the first inner solve (the guess costs one more operator
-                                application for its residual).  FP64: any non-zero value = initial guess
+                                MIXED: 1 = left preconditioner of the first inner solve (the later corrections
+                                solve the plain operator), 2 = preconditioner and initial guess of the first
+                                inner solve (the guess costs one more operator application for its residual).  FP64: any non-zero value = initial guess
                                 x0 only (the Krylov iteration and stopping test stay the reference's). */
   int32_t verbose;           /* print per-cycle diagnostics like krylov_block.rs:148-151 (default 0) */
   int64_t aux_chunk;         /* aux functions per K-term chunk (default 0 = automatic) */
@@ -78,7 +78,7 @@ typedef struct cphf_config {
                                 operator of residual_dfloat: with the exact-slice tensor cores (residual_dfloat
                                 = 2) as r -= (I + A) d, the correction d applied in correction precision:
                                 the fewest BF16 slices per operand whose error bound (3 slices, 6
-                                exact-accumulated products: ~2^-12 |r|; 4 slices, 10 products: ~2^-18 |r|)
+                                exact-accumulated products: ~2^-14 |r|; 4 slices, 10 products: ~2^-20 |r|)
                                 stays below 0.1 residual_tol, else all six; otherwise recomputed in full.
                                 With 1 or 2 the solve returns only after such a max_j ||b_j - (I+A)x_j||_2
                                 < residual_tol. */

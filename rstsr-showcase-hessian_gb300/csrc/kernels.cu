@@ -449,37 +449,6 @@ void launch_mgs(double* V, int64_t n, int64_t m, double lindep, double* ip, int*
   }
 }
 
-namespace {
-// |x| of non-negative doubles orders like their bit patterns: min / max by integer atomics
-__global__ void abs_minmax_kernel(const double* __restrict__ x, int64_t n, unsigned long long* out) {
-  unsigned long long lo = ~0ull, hi = 0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const unsigned long long k = (unsigned long long)__double_as_longlong(x[i]) & 0x7FFFFFFFFFFFFFFFull;
-    lo = min(lo, k);
-    hi = max(hi, k);
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicMin(out, lo);
-    atomicMax(out + 1, hi);
-  }
-}
-__global__ void minmax_init_kernel(unsigned long long* out) {
-  out[0] = ~0ull;
-  out[1] = 0;
-}
-}  // namespace
-
-void launch_abs_minmax(const double* x, int64_t n, double* out, cudaStream_t s) {
-  unsigned long long* o = reinterpret_cast<unsigned long long*>(out);
-  minmax_init_kernel<<<1, 1, 0, s>>>(o);
-  abs_minmax_kernel<<<grid_for(n), kThreads, 0, s>>>(x, n, o);
-  count_launch(2);
-}
-
 void launch_gather_cols(const double* src, int64_t n, const int* idx, int64_t cnt, double* dst,
                         int64_t ld_dst, cudaStream_t s) {
   if (cnt <= 0) return;

@@ -37,8 +37,6 @@ void launch_to_f32(const double* src, int64_t n, float* dst, cudaStream_t s);
 
 // r[:, j] = b[:, j] - x[:, j] - ax[:, j] (any pointer may alias r); norms2[j] = ||r[:, j]||^2
 // (deterministic two-level reduction).  `partials` needs nblocks_for(n) * nb doubles.
-// out[0] = min |x_i|, out[1] = max |x_i| over i < n (device)
-void launch_abs_minmax(const double* x, int64_t n, double* out, cudaStream_t s);
 void launch_residual_norms(const double* b, const double* x, const double* ax, double* r,
                            int64_t n, int64_t nb, double* norms2, double* partials,
                            cudaStream_t s);
