@@ -210,10 +210,13 @@ def test_solve_dimless_cphf_fp64_matches_oracle(dims):
 
 
 TC_RAGGED = dict(nao=150, naux=70, nocc=(13,), natm=9, decay=12.0)
+# more than 128 occupied orbitals: the inner T generation leaves the bra-resident kernel for the
+# batched one (K = nocc over more than four blocks of 32)
+TC_WIDE_OCC = dict(nao=176, naux=60, nocc=(136,), natm=2, decay=12.0)
 
 
 @pytest.mark.parametrize("tc", [1, 0])
-@pytest.mark.parametrize("dims", [MEDIUM, TC_RAGGED, MEDIUM_U, GRID_R, GRID_U])
+@pytest.mark.parametrize("dims", [MEDIUM, TC_RAGGED, TC_WIDE_OCC, MEDIUM_U, GRID_R, GRID_U])
 def test_lowp_operator_accuracy(dims, tc):
     """The split-precision operator of the mixed solve agrees with FP64 to LOWP_TOL."""
     s = synth.make_system(dims, seed=14)
