@@ -25,7 +25,9 @@ struct Exact6 {
 // accumulation bounds; with NS = 3 the fourth accumulator stays unused.
 template <int NS>
 struct ExactC {
-  static constexpr int S = NS, NACC = 4, EOFF = 0, STAGES = 3;
+  // split-K stages of 16 KB per plane pair: 3 x 64 KB (NS = 4) or 4 x 48 KB (NS = 3), so the
+  // fewer products per stage still cover the loads' latency
+  static constexpr int S = NS, NACC = 4, EOFF = 0, STAGES = NS == 3 ? 4 : 3;
   static constexpr bool BF16 = true;
   using Elem = __nv_bfloat16;
 };

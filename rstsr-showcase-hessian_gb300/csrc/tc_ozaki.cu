@@ -350,7 +350,9 @@ __global__ void __launch_bounds__(128, 1)
 template <class PR>
 struct Batched {
   static constexpr int BN = 64;
-  static constexpr int STAGES = PR::S == 6 ? 2 : 3;  // 6 exact slices: 2 stages; 4 slices / split FP16: 3
+  // stages of S x 12 KB: as many as the shared memory of the one CTA per SM holds for the exact
+  // slices (3 x 72 KB, 4 x 48 KB, 5 x 36 KB); split FP16 (two CTAs per SM): 3 x 24 KB
+  static constexpr int STAGES = PR::NACC == 4 ? (PR::S == 6 ? 3 : PR::S == 4 ? 4 : 5) : 3;
   static constexpr int THREADS = 320;
   static constexpr int EPI_WARPS = 8;
   static constexpr int SMEM_BYTES = STAGES * Cfg<PR, BN>::STAGE_BYTES + 1024 + 1024;
