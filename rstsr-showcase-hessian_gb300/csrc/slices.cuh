@@ -100,33 +100,14 @@ __device__ __forceinline__ void slice6(double x, int e, __nv_bfloat16* dst, int6
   const long long F = fix_round(x, 36 - e, bad);
   digits6<NS>(F, bad, dst, plane);
 }
-// Digits of an FP32 pair v = x.x + x.y (|v| < 2^e) in FP32 arithmetic: the balanced base-64
-// digits of F ~ v 2^(36 - e) (|F - v 2^(36 - e)| <= 1/2 + 2^-6), the same representation as
-// the integer path above at a fraction of its instructions.  The high part alone gives the
-// first three digits: its remainders r = r - q 2^s stay exact (multiples of its ulp with at
-// most 24 significant bits); the low part (below the high part's ulp) joins once the
-// remainder is below 2^17, where their sum keeps 2^-6 resolution; q_t = rint(r 2^-s) is
-// balanced, |q_0| <= 64, |q_t| <= 32.
-template <int NS = 6>
-__device__ __forceinline__ void slice6(float2 x, int e, __nv_bfloat16* dst, int64_t plane) {
-  const bool bad = !isfinite(x.x) || !isfinite(x.y);
-  float r = ldexpf(x.x, 36 - e);
-  const float lo = ldexpf(x.y, 36 - e);
-#pragma unroll
-  for (int t = 0; t < NS; ++t) {
-    if (t == 3) r += lo;
-    const int sh = 30 - 6 * t;
-    const float unit = __int_as_float((127 + sh) << 23);          // 2^sh
-    const float q = rintf(r * __int_as_float((127 - sh) << 23));  // r 2^-sh
-    r = fmaf(-q, unit, r);
-    float v = q * __int_as_float((127 - 6 * (t + 1)) << 23);     // q 2^(-6(t+1)), exact
-    if (bad) v = __int_as_float(0x7FC00000);
-    dst[t * plane] = __float2bfloat16_rn(v);
-  }
-}
-
-// The same digits of an FP32 pair already scaled by 2^(36 - e) (x f1 f2, f1 f2 = 2^(36 - e)
-// as two normal powers of two, so that no ldexpf is needed), into d[0 .. NS).
+// Digits of an FP32 pair v = hi + lo (|v| < 2^e) in FP32 arithmetic, into d[0 .. NS): the
+// balanced base-64 digits of F ~ v 2^(36 - e) (|F - v 2^(36 - e)| <= 1/2 + 2^-6), the same
+// representation as the integer path above at a fraction of its instructions.  The scale
+// comes as two normal powers of two f1 f2 = 2^(36 - e), so that no ldexpf is needed.  The high
+// part alone gives the first three digits: its remainders r = r - q 2^s stay exact (multiples
+// of its ulp with at most 24 significant bits); the low part (below the high part's ulp) joins
+// once the remainder is below 2^17, where their sum keeps 2^-6 resolution; q_t = rint(r 2^-s)
+// is balanced, |q_0| <= 64, |q_t| <= 32.
 template <int NS>
 __device__ __forceinline__ void digits_pair(float hi, float lo, float f1, float f2, float* d) {
   const bool bad = !isfinite(hi) || !isfinite(lo);
@@ -152,7 +133,6 @@ struct Put<Exact6> {
 };
 template <int NS>
 struct Put<ExactC<NS>> {  // only the planes a correction-precision product reads
-  __device__ static void put(float2 x, int e, __nv_bfloat16* dst, int64_t plane) { slice6<NS>(x, e, dst, plane); }
   __device__ static void put(double x, int e, __nv_bfloat16* dst, int64_t plane) { slice6<NS>(x, e, dst, plane); }
 };
 template <>
