@@ -313,9 +313,11 @@ cphf_status cphf_rij_response_bra_noalloc(const double* Z, const double* bra, in
  * W1[64,3] b1[64] W2[64,64] b2[64] W3[2,64] b3[2] (row-major per matrix), 4546 floats.
  * Sample features [n, 3] (row-major): gap e_a - e_i, dimensionless RHS entry b, (ia|ia).
  * Outputs [n, 2]: o1 (initial guess x0 = b (1 + o1)), o2 (effective diagonal d of the
- * dimensionless operator; preconditioner 1 / (1 + d)).  With use_learned_guess set, the
- * solve starts from the guess and left-preconditions the Krylov iteration; the unmodified
- * operator still defines convergence (mixed: the FP64 residual), so the answer is unchanged. */
+ * dimensionless operator; preconditioner 1 / (1 + d)).  With use_learned_guess set, a mixed
+ * solve left-preconditions its first inner solve (1) and also starts it from the guess (2); an
+ * FP64 solve only starts from the guess.  The unmodified operator still defines convergence
+ * (mixed: the FP64-accurate residual; FP64: the reference's stopping test), so the answer is
+ * unchanged. */
 cphf_status cphf_mlp_set_weights(cphf_ctx* ctx, const float* weights, int64_t nweights);
 cphf_status cphf_mlp_get_weights(cphf_ctx* ctx, float* weights, int64_t nweights);
 /* Features of every (vir a, occ i, column r) sample of rhs[s] [nmo, nocc_s, nprop]
