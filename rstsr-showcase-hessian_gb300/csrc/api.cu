@@ -601,8 +601,8 @@ cphf_status cphf_solve_dimless_cphf(cphf_ctx* c, const double* const* rhs, int64
     if (x0) pack_krylov(c, x0, nprop, xg);
     const double* x0p = x0 ? xg : nullptr;
     // Learned initial guess / left preconditioner, in context-owned buffers (no allocation per
-    // solve).  Mixed precision: the preconditioner m acts on the inner solves only, whose
-    // convergence the outer FP64-accurate residual judges; mode 2 also starts the first inner
+    // solve).  Mixed precision: the preconditioner m acts on the first inner solve only, whose
+    // convergence the outer FP64-accurate residual decides; mode 2 also starts the first inner
     // solve from the guess (one more operator application for its residual).  FP64: the guess
     // is only the initial x0, so the Krylov iteration and its stopping test are the
     // reference's unmodified ones (krylov_block.rs:86-87, 130-157).
